@@ -1,0 +1,144 @@
+/*
+ * plbm_gpu.h -- C ABI of libplbmgpu.so, the GB300 (sm_103a) D2Q9 periodic
+ * stream-collide library.
+ *
+ * Every entry point takes plain pointers and sizes, returns 0 (PLBM_OK) or a
+ * negative PLBM_E* code, and records a message readable through
+ * plbm_last_error() (thread-local).  A handle is not reentrant: calls on one
+ * handle must be serialised by the caller (the reference calls one routine at
+ * a time from its serial time loop).  Distinct handles are independent.
+ *
+ * Lattice layout is the reference's (src/fvm_bardow.F90:144-153):
+ *   f(ld,nx,0:8,nf), element (y,x,q,b) at 0-based offset
+ *   y + ld*(x + nx*(q + 9*b)), ld = ny rounded up to a multiple of 16.
+ * Macroscopic fields are (ny,nx) arrays, y fastest (src/fvm_bardow.F90:155).
+ * Buffer indices (iold, inew, ibuf) are 1-based, as in the Fortran.
+ */
+#ifndef PLBM_GPU_H
+#define PLBM_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define PLBM_OK             0
+#define PLBM_E_INVALID     -1  /* bad argument: size, kind, index, NULL     */
+#define PLBM_E_NOMEM       -2  /* device or pinned allocation failed        */
+#define PLBM_E_CUDA        -3  /* CUDA runtime error (message has details)  */
+#define PLBM_E_UNSUPPORTED -4  /* valid request this build does not offer   */
+#define PLBM_E_TIMEOUT     -5  /* a bounded device-side wait expired        */
+#define PLBM_E_NODEVICE    -6  /* no CUDA device visible                    */
+
+/* ---- collision kinds (grid%collision => collide_*) ---------------------- */
+#define PLBM_BGK   0  /* collide_bgk, src/collision_bgk.F90:17-82          */
+#define PLBM_TRT   1  /* collide_trt, src/collision_trt.F90:41-160         */
+#define PLBM_RR    2  /* collide_rr,  src/collision_regularized.F90:21-202 */
+#define PLBM_BGKI  3  /* collide_bgk_improved, src/collision_bgk_improved.f90:16-109 */
+
+/* ---- storage of the populations on the device -------------------------- */
+#define PLBM_F64     0  /* f_i in binary64, reference semantics               */
+#define PLBM_F32DEV  1  /* h_i = f_i - w_i in binary32, binary32 collision     */
+#define PLBM_F16DEV  2  /* h_i = f_i - w_i in binary16 scaled by 2^PLBM_F16_SCALE_LOG2 */
+#define PLBM_F16_SCALE_LOG2 15
+
+/* ---- arithmetic of the PLBM_F64 kernels -------------------------------- */
+#define PLBM_MATH_FMA    0  /* binary64, FMA contraction allowed (default)   */
+#define PLBM_MATH_STRICT 1  /* binary64, no contraction: same operations and */
+                            /* order as the Fortran, bit-identical to it     */
+#define PLBM_MATH_DF64   2  /* binary64 storage, arithmetic in unevaluated   */
+                            /* float pairs (hi+lo) on the FP32 pipe          */
+
+typedef struct plbm_grid plbm_grid_t;
+
+/* Message of the last failing call on this thread ("" if none). */
+const char *plbm_last_error(void);
+/* Library ABI version (major*10000 + minor*100 + patch). */
+int plbm_version(void);
+
+/* ---- lattice_grid lifecycle -------------------------------------------- */
+/* alloc_grid(grid,nx,ny,nf) -- src/fvm_bardow.F90:129-202.  Allocates nf
+ * device lattices (ld,nx,0:8), sets inew=1, iold=2, collision BGK.  nf >= 2. */
+int plbm_grid_create(int nx, int ny, int nf, int storage, plbm_grid_t **out);
+/* dealloc_grid -- src/fvm_bardow.F90:204-240.  NULL is accepted. */
+int plbm_grid_destroy(plbm_grid_t *g);
+int plbm_grid_info(const plbm_grid_t *g, int *nx, int *ny, int *ld, int *nf, int *storage);
+/* grid%iold / grid%inew (1-based). */
+int plbm_grid_indices(const plbm_grid_t *g, int *iold, int *inew);
+int plbm_grid_set_indices(plbm_grid_t *g, int iold, int inew);
+/* Run the handle's work on this cudaStream_t (NULL = the handle's own stream). */
+int plbm_grid_set_stream(plbm_grid_t *g, void *cuda_stream);
+/* Device address of lattice ibuf (for device-resident callers). */
+int plbm_grid_device_ptr(const plbm_grid_t *g, int ibuf, void **dptr);
+
+/* ---- properties --------------------------------------------------------- */
+/* set_properties(grid,nu,dt[,magic]) -- src/fvm_bardow.F90:242-269.
+ * tau = 3 nu, omega = dt/(tau + dt/2), trt_magic = magic or (tau/dt)^2.
+ * magic may be NULL (absent optional). */
+int plbm_set_properties(plbm_grid_t *g, double nu, double dt, const double *magic);
+int plbm_get_properties(const plbm_grid_t *g, double *nu, double *dt, double *tau,
+                        double *omega, double *trt_magic);
+/* Set omega and the TRT magic parameter directly. */
+int plbm_set_relaxation(plbm_grid_t *g, double omega, double trt_magic);
+/* grid%collision => collide_bgk | collide_trt | collide_rr | collide_bgk_improved
+ * (app/main_taylor_green.f90:39). */
+int plbm_set_collision(plbm_grid_t *g, int kind);
+/* PLBM_MATH_* for PLBM_F64 storage. */
+int plbm_set_math(plbm_grid_t *g, int math);
+
+/* ---- transfers ---------------------------------------------------------- */
+/* Copy host f(:,:,:,ibuf) (ld*nx*9 doubles) to/from the device lattice.
+ * For deviation storage the values are converted (f - w_i) on the device. */
+int plbm_upload(plbm_grid_t *g, const double *f_host, int ibuf);
+int plbm_download(plbm_grid_t *g, double *f_host, int ibuf);
+
+/* ---- the hot path ------------------------------------------------------- */
+/* set_pdf_to_equilibrium -- src/fvm_bardow.F90:272-305.  rho, ux, uy are host
+ * (ny,nx) arrays; writes the equilibrium into f(:,:,:,iold) on the device. */
+int plbm_set_pdf_to_equilibrium(plbm_grid_t *g, const double *rho, const double *ux,
+                                const double *uy);
+/* lbm_stream -- src/periodic_lbm.f90:32-129: f(:,:,:,iold) -> f(:,:,:,inew). */
+int plbm_stream(plbm_grid_t *g);
+/* grid%collision() -- in place on f(:,:,:,inew). */
+int plbm_collide(plbm_grid_t *g);
+/* perform_lbm_step -- src/periodic_lbm.f90:15-29, nsteps times: one fused
+ * pull-stream + collide kernel per step, then the iold/inew swap. */
+int plbm_perform_lbm_step(plbm_grid_t *g, int nsteps);
+/* update_macros -- src/fvm_bardow.F90:343-390: moments of f(:,:,:,inew)
+ * into host (ny,nx) arrays.  Any of rho/ux/uy may be NULL. */
+int plbm_update_macros(plbm_grid_t *g, double *rho, double *ux, double *uy);
+/* Same moments of lattice ibuf into DEVICE (ny,nx) arrays, asynchronous. */
+int plbm_macros_device(plbm_grid_t *g, int ibuf, double *rho, double *ux, double *uy);
+
+/* ---- vorticity, src/vorticity.f90 --------------------------------------- */
+/* vorticity_2nd (order 2, :13-43) or vorticity_4th (order 4, :46-87) on host
+ * (ny,nx) arrays.  order 44 selects the standard 4th-order weights (2/3 on
+ * +-1, -1/12 on +-2), which the reference routine does not use. */
+int plbm_vorticity(int order, int nx, int ny, const double *ux, const double *uy, double *omega);
+/* Same on device arrays, asynchronous on cuda_stream (may be NULL). */
+int plbm_vorticity_device(int order, int nx, int ny, const double *ux, const double *uy,
+                          double *omega, void *cuda_stream);
+
+/* ---- binary64 reductions ------------------------------------------------- */
+/* E = 1/2 sum rho |u|^2 over the moments of lattice ibuf (moments evaluated as
+ * in update_macros), accumulated in binary64. */
+int plbm_kinetic_energy(plbm_grid_t *g, int ibuf, double *energy);
+/* sqrt(sum |u - ua|^2 / sum |ua|^2) for lattice ibuf against host (ny,nx)
+ * fields uxa, uya (calc_L2_norm, app/main_taylor_green.f90:174-212). */
+int plbm_velocity_l2_error(plbm_grid_t *g, int ibuf, const double *uxa, const double *uya,
+                           double *err);
+
+/* Wait for all work queued on the handle's stream. */
+int plbm_synchronize(plbm_grid_t *g);
+
+/* ---- raw device launches (device-resident callers: batched, autograd) ---- */
+/* One fused pull-stream + collide step over device lattices fsrc -> fdst
+ * (layout above, PLBM_F64 storage = double, F32DEV = float, F16DEV = half). */
+int plbm_launch_step(int storage, int math, int kind, int nx, int ny, int ld,
+                     const void *fsrc, void *fdst, double omega, double trt_magic,
+                     void *cuda_stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PLBM_GPU_H */

@@ -1,0 +1,58 @@
+/*
+ * plbm_plugin.h -- the reference's simulation-plugin C ABI, served by
+ * libplbmgpu.so under the stem "plbmgpu".
+ *
+ * Replaces the Fortran plugin sim/sim_slbm.F90:155-228 (prototypes in
+ * sim/lbm.h:13-19).  A loader derives the symbol names from the library file
+ * stem (sim/cases.py:21-32): libplbmgpu.so -> c_plbmgpu_{init,step,vars,free,norm}.
+ *
+ * Semantics follow sim/sim_slbm.F90 and sim/sim.F90:
+ *  - fields are (nx,ny) arrays, x fastest (Fortran order); u is (nx,ny,2);
+ *  - the "rho" argument of init carries the pressure p, and the density is
+ *    rho = 1 + p/cs^2 (sim/sim.F90:193, sim/cases.py:302-303);
+ *  - populations are stored shifted, h_i = f_i - w_i (sim/sim.F90:131,384);
+ *  - a step is collide-then-push-stream with periodic wrap
+ *    (sim/sim.F90:404-505 + :568-624);
+ *  - dt must be 1.0 (sim/sim_slbm.F90:71-74).
+ * Where the reference stops the program (error stop), these entry points
+ * return NULL / set a sticky error instead; read it with plbm_last_error()
+ * and c_plbmgpu_status().
+ */
+#ifndef PLBM_PLUGIN_H
+#define PLBM_PLUGIN_H
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Optional plugin parameters, passed through the params slot of init
+ * (the reference passes NULL there, sim/cases.py:95).  NULL selects
+ * {BGK, PLBM_F64, trt_magic 0.25}. */
+typedef struct plbm_plugin_params {
+    int version;       /* 1, or 2 when `math` is filled in                  */
+    int kind;          /* PLBM_BGK | PLBM_TRT | PLBM_RR                    */
+    int storage;       /* PLBM_F64 | PLBM_F32DEV | PLBM_F16DEV             */
+    double trt_magic;  /* TRT magic parameter (Lambda)                     */
+    int math;          /* version 2: PLBM_MATH_FMA | PLBM_MATH_STRICT      */
+} plbm_plugin_params;
+
+/* siminit -- sim/lbm.h:13-15, sim/sim_slbm.F90:158-172 */
+void *c_plbmgpu_init(int nx, int ny, double dt, const double *rho, const double *u,
+                     const double *sigma, void *params);
+/* simstep -- sim/lbm.h:17, sim/sim_slbm.F90:175-183 */
+void c_plbmgpu_step(void *sim, double omega);
+/* simvars -- sim/lbm.h:18, sim/sim_slbm.F90:186-203 */
+void c_plbmgpu_vars(void *sim, double *rho, double *u);
+/* simfree -- sim/lbm.h:19, sim/sim_slbm.F90:207-218 */
+void c_plbmgpu_free(void *sim);
+/* norm2(u-ua)/norm2(ua) -- sim/sim_slbm.F90:221-228 (host arithmetic) */
+double c_plbmgpu_norm(int nx, int ny, const double *u, const double *ua);
+/* Not in the reference: sticky status of a plugin instance (0 = ok). */
+int c_plbmgpu_status(void *sim);
+/* Not in the reference: run nsteps steps in one call (same result as nsteps
+ * calls of c_plbmgpu_step). */
+int c_plbmgpu_steps(void *sim, double omega, int nsteps);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

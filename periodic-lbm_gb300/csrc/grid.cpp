@@ -1,0 +1,540 @@
+// grid.cpp -- the plbm_* C ABI: a device-resident mirror of the reference's
+// lattice_grid (src/fvm_bardow.F90:37-69) and the routines that act on it.
+//
+// The handle owns `nf` device lattices of the reference layout f(ld,nx,0:8)
+// and the integer buffer indices iold/inew (1-based, as in the Fortran).  The
+// host copy of grid%f stays with the caller; transfers happen only in
+// plbm_upload / plbm_download / plbm_update_macros.
+//
+// Compiled with -ffp-contract=off so that the scalar relaxation parameters
+// (omega, lambda_d, w*(1-omega), ...) are the same binary64 values the
+// Fortran computes.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+#include <string>
+#include <vector>
+
+#include "../../include/plbm_gpu.h"
+#include "plbm_launch.h"
+
+using namespace plbm;
+
+// ---------------------------------------------------------------------------
+// error reporting
+namespace plbm_internal {
+thread_local std::string g_last_error;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+int cuda_fail(cudaError_t e, const char* what) {
+  const int code = e == cudaErrorMemoryAllocation ? PLBM_E_NOMEM
+                   : e == cudaErrorNotSupported   ? PLBM_E_UNSUPPORTED
+                                                  : PLBM_E_CUDA;
+  return fail(code, "%s: %s (%s)", what, cudaGetErrorString(e), cudaGetErrorName(e));
+}
+int ok() { return PLBM_OK; }
+}  // namespace plbm_internal
+using namespace plbm_internal;
+
+#define CUDA_TRY(expr, what)                \
+  do {                                      \
+    cudaError_t e_ = (expr);                \
+    if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+  } while (0)
+
+extern "C" const char* plbm_last_error(void) { return g_last_error.c_str(); }
+extern "C" int plbm_version(void) { return 1 * 10000 + 0 * 100 + 0; }
+
+// ---------------------------------------------------------------------------
+struct plbm_grid {
+  int nx, ny, ld, nf, storage;
+  int kind = PLBM_BGK, math = PLBM_MATH_FMA;
+  int iold = 2, inew = 1;
+  double nu = 0, dt = 1, tau = 0, omega = 1, trt_magic = 0.25;
+  int device = 0;
+  void* f = nullptr;           // nf lattices, contiguous
+  size_t lat_elems = 0;        // ld*nx*9
+  size_t elem_bytes = 8;
+  cudaStream_t own = nullptr;  // stream created by the handle
+  cudaStream_t stream = nullptr;
+  double* scratch = nullptr;   // 3*nx*ny doubles + reduction partials
+  size_t scratch_elems = 0;
+};
+
+namespace {
+
+int pad16(int n) {
+  int r = n % 16;
+  return r > 0 ? n + (16 - r) : n;
+}
+
+int check_grid(const plbm_grid_t* g) {
+  if (!g) return fail(PLBM_E_INVALID, "NULL grid handle");
+  return PLBM_OK;
+}
+
+int check_buf(const plbm_grid_t* g, int ibuf) {
+  if (ibuf < 1 || ibuf > g->nf) return fail(PLBM_E_INVALID, "buffer index %d outside 1..%d", ibuf, g->nf);
+  return PLBM_OK;
+}
+
+void* lattice(const plbm_grid_t* g, int ibuf) {
+  return static_cast<char*>(g->f) + (size_t)(ibuf - 1) * g->lat_elems * g->elem_bytes;
+}
+
+int use_device(const plbm_grid_t* g) {
+  CUDA_TRY(cudaSetDevice(g->device), "cudaSetDevice");
+  return PLBM_OK;
+}
+
+int ensure_scratch(plbm_grid_t* g, size_t elems) {
+  if (g->scratch_elems >= elems) return PLBM_OK;
+  if (g->scratch) cudaFree(g->scratch);
+  g->scratch = nullptr;
+  g->scratch_elems = 0;
+  CUDA_TRY(cudaMalloc(&g->scratch, elems * sizeof(double)), "cudaMalloc(scratch)");
+  g->scratch_elems = elems;
+  return PLBM_OK;
+}
+
+int internal_storage(int storage) { return storage; }  // PLBM_F64/F32DEV/F16DEV == ST_*
+
+}  // namespace
+
+// Relaxation parameters of one launch, as the Fortran forms them:
+//   BGK  omegabar = 1 - omega                      (src/collision_bgk.F90:26)
+//   TRT  lambda_e = omega, lambda_d(omega, magic)  (src/collision_trt.F90:47-48)
+//   RR   w*(1 - omega)                             (src/collision_regularized.F90:63-65)
+//   BGKI fac = 4.5 - 2.25*omega                    (src/collision_bgk_improved.f90:39)
+CollParams plbm_make_params(double omega, double trt_magic) {
+  CollParams p;
+  p.omega = omega;
+  p.omegabar = 1.0 - omega;
+  p.lambda_d = (4.0 - 2.0 * omega) / (4.0 * trt_magic * omega + 2.0 - omega);
+  p.les = 0.5 * omega;
+  p.lds = 0.5 * p.lambda_d;
+  p.rr_w0 = W0 * (1.0 - omega);
+  p.rr_ws = WS * (1.0 - omega);
+  p.rr_wd = WD * (1.0 - omega);
+  p.bgki_fac = 4.5 - 2.25 * omega;
+  return p;
+}
+
+extern "C" int plbm_grid_create(int nx, int ny, int nf, int storage, plbm_grid_t** out) {
+  if (!out) return fail(PLBM_E_INVALID, "out is NULL");
+  *out = nullptr;
+  if (nx < 1 || ny < 1) return fail(PLBM_E_INVALID, "grid size %dx%d: nx and ny must be >= 1", nx, ny);
+  if (nf < 2 || nf > 16) return fail(PLBM_E_INVALID, "nf = %d: need 2 <= nf <= 16", nf);
+  if (storage != PLBM_F64 && storage != PLBM_F32DEV && storage != PLBM_F16DEV)
+    return fail(PLBM_E_INVALID, "unknown storage %d", storage);
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+    cudaGetLastError();
+    return fail(PLBM_E_NODEVICE, "no CUDA device visible");
+  }
+  const int ld = pad16(ny);
+  const size_t lat = (size_t)ld * (size_t)nx * 9u;
+  if ((double)lat * nf > 4.0e11) return fail(PLBM_E_INVALID, "lattice of %zu elements x %d is too large", lat, nf);
+  plbm_grid_t* g = new plbm_grid_t();
+  g->nx = nx;
+  g->ny = ny;
+  g->ld = ld;
+  g->nf = nf;
+  g->storage = storage;
+  g->lat_elems = lat;
+  g->elem_bytes = storage == PLBM_F64 ? 8 : (storage == PLBM_F32DEV ? 4 : 2);
+  cudaGetDevice(&g->device);
+  cudaError_t e = cudaMalloc(&g->f, lat * nf * g->elem_bytes);
+  if (e != cudaSuccess) {
+    delete g;
+    cudaGetLastError();
+    return cuda_fail(e, "cudaMalloc(lattices)");
+  }
+  // allocate() leaves the Fortran array undefined; zero is a deterministic stand-in.
+  e = cudaMemset(g->f, 0, lat * nf * g->elem_bytes);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&g->own, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    cudaFree(g->f);
+    delete g;
+    return cuda_fail(e, "grid setup");
+  }
+  g->stream = g->own;
+  *out = g;
+  return ok();
+}
+
+extern "C" int plbm_grid_destroy(plbm_grid_t* g) {
+  if (!g) return PLBM_OK;
+  cudaSetDevice(g->device);
+  cudaStreamSynchronize(g->stream);
+  if (g->f) cudaFree(g->f);
+  if (g->scratch) cudaFree(g->scratch);
+  if (g->own) cudaStreamDestroy(g->own);
+  delete g;
+  return PLBM_OK;
+}
+
+extern "C" int plbm_grid_info(const plbm_grid_t* g, int* nx, int* ny, int* ld, int* nf, int* storage) {
+  if (int r = check_grid(g)) return r;
+  if (nx) *nx = g->nx;
+  if (ny) *ny = g->ny;
+  if (ld) *ld = g->ld;
+  if (nf) *nf = g->nf;
+  if (storage) *storage = g->storage;
+  return PLBM_OK;
+}
+
+extern "C" int plbm_grid_indices(const plbm_grid_t* g, int* iold, int* inew) {
+  if (int r = check_grid(g)) return r;
+  if (iold) *iold = g->iold;
+  if (inew) *inew = g->inew;
+  return PLBM_OK;
+}
+
+extern "C" int plbm_grid_set_indices(plbm_grid_t* g, int iold, int inew) {
+  if (int r = check_grid(g)) return r;
+  if (int r = check_buf(g, iold)) return r;
+  if (int r = check_buf(g, inew)) return r;
+  if (iold == inew) return fail(PLBM_E_INVALID, "iold and inew must differ");
+  g->iold = iold;
+  g->inew = inew;
+  return PLBM_OK;
+}
+
+extern "C" int plbm_grid_set_stream(plbm_grid_t* g, void* s) {
+  if (int r = check_grid(g)) return r;
+  g->stream = s ? static_cast<cudaStream_t>(s) : g->own;
+  return PLBM_OK;
+}
+
+extern "C" int plbm_grid_device_ptr(const plbm_grid_t* g, int ibuf, void** dptr) {
+  if (int r = check_grid(g)) return r;
+  if (int r = check_buf(g, ibuf)) return r;
+  if (!dptr) return fail(PLBM_E_INVALID, "dptr is NULL");
+  *dptr = lattice(g, ibuf);
+  return PLBM_OK;
+}
+
+extern "C" int plbm_set_properties(plbm_grid_t* g, double nu, double dt, const double* magic) {
+  if (int r = check_grid(g)) return r;
+  if (!(dt > 0.0) || !(nu > 0.0)) return fail(PLBM_E_INVALID, "nu and dt must be > 0 (nu=%g dt=%g)", nu, dt);
+  // src/fvm_bardow.F90:249-265
+  const double csqr = 1.0 / 3.0, invcsqr = 1.0 / csqr;
+  g->nu = nu;
+  g->dt = dt;
+  const double tau = invcsqr * nu;
+  g->tau = tau;
+  g->omega = dt / (tau + 0.5 * dt);
+  if (magic) g->trt_magic = *magic;
+  else {
+    const double r = tau / dt;
+    g->trt_magic = r * r;
+  }
+  return PLBM_OK;
+}
+
+extern "C" int plbm_get_properties(const plbm_grid_t* g, double* nu, double* dt, double* tau, double* omega,
+                                   double* trt_magic) {
+  if (int r = check_grid(g)) return r;
+  if (nu) *nu = g->nu;
+  if (dt) *dt = g->dt;
+  if (tau) *tau = g->tau;
+  if (omega) *omega = g->omega;
+  if (trt_magic) *trt_magic = g->trt_magic;
+  return PLBM_OK;
+}
+
+extern "C" int plbm_set_relaxation(plbm_grid_t* g, double omega, double trt_magic) {
+  if (int r = check_grid(g)) return r;
+  if (!(omega > 0.0 && omega < 2.0)) return fail(PLBM_E_INVALID, "omega = %g outside (0,2)", omega);
+  g->omega = omega;
+  g->trt_magic = trt_magic;
+  return PLBM_OK;
+}
+
+extern "C" int plbm_set_collision(plbm_grid_t* g, int kind) {
+  if (int r = check_grid(g)) return r;
+  if (kind < PLBM_BGK || kind > PLBM_BGKI) return fail(PLBM_E_INVALID, "unknown collision kind %d", kind);
+  if (kind == PLBM_BGKI && g->storage != PLBM_F64)
+    return fail(PLBM_E_UNSUPPORTED, "collide_bgk_improved is offered for PLBM_F64 storage only");
+  g->kind = kind;
+  return PLBM_OK;
+}
+
+extern "C" int plbm_set_math(plbm_grid_t* g, int math) {
+  if (int r = check_grid(g)) return r;
+  if (math < PLBM_MATH_FMA || math > PLBM_MATH_DF64) return fail(PLBM_E_INVALID, "unknown math mode %d", math);
+  g->math = math;
+  return PLBM_OK;
+}
+
+// ---------------------------------------------------------------------------
+extern "C" int plbm_upload(plbm_grid_t* g, const double* f_host, int ibuf) {
+  if (int r = check_grid(g)) return r;
+  if (int r = check_buf(g, ibuf)) return r;
+  if (!f_host) return fail(PLBM_E_INVALID, "f_host is NULL");
+  if (int r = use_device(g)) return r;
+  const size_t bytes64 = g->lat_elems * sizeof(double);
+  if (g->storage == PLBM_F64) {
+    CUDA_TRY(cudaMemcpyAsync(lattice(g, ibuf), f_host, bytes64, cudaMemcpyHostToDevice, g->stream), "upload");
+    CUDA_TRY(cudaStreamSynchronize(g->stream), "upload sync");
+    return ok();
+  }
+  double* tmp = nullptr;
+  CUDA_TRY(cudaMalloc(&tmp, bytes64), "cudaMalloc(upload staging)");
+  cudaError_t e = cudaMemcpyAsync(tmp, f_host, bytes64, cudaMemcpyHostToDevice, g->stream);
+  if (e == cudaSuccess) e = f64_to_dev(internal_storage(g->storage), g->nx, g->ny, g->ld, tmp, lattice(g, ibuf), g->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+  cudaFree(tmp);
+  if (e != cudaSuccess) return cuda_fail(e, "upload (deviation conversion)");
+  return ok();
+}
+
+extern "C" int plbm_download(plbm_grid_t* g, double* f_host, int ibuf) {
+  if (int r = check_grid(g)) return r;
+  if (int r = check_buf(g, ibuf)) return r;
+  if (!f_host) return fail(PLBM_E_INVALID, "f_host is NULL");
+  if (int r = use_device(g)) return r;
+  const size_t bytes64 = g->lat_elems * sizeof(double);
+  if (g->storage == PLBM_F64) {
+    CUDA_TRY(cudaMemcpyAsync(f_host, lattice(g, ibuf), bytes64, cudaMemcpyDeviceToHost, g->stream), "download");
+    CUDA_TRY(cudaStreamSynchronize(g->stream), "download sync");
+    return ok();
+  }
+  double* tmp = nullptr;
+  CUDA_TRY(cudaMalloc(&tmp, bytes64), "cudaMalloc(download staging)");
+  // padding rows are not converted; give them a defined value
+  cudaError_t e = cudaMemsetAsync(tmp, 0, bytes64, g->stream);
+  if (e == cudaSuccess) e = dev_to_f64(internal_storage(g->storage), g->nx, g->ny, g->ld, lattice(g, ibuf), tmp, g->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(f_host, tmp, bytes64, cudaMemcpyDeviceToHost, g->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+  cudaFree(tmp);
+  if (e != cudaSuccess) return cuda_fail(e, "download (deviation conversion)");
+  return ok();
+}
+
+extern "C" int plbm_set_pdf_to_equilibrium(plbm_grid_t* g, const double* rho, const double* ux, const double* uy) {
+  if (int r = check_grid(g)) return r;
+  if (!rho || !ux || !uy) return fail(PLBM_E_INVALID, "rho, ux and uy must be non-NULL");
+  if (int r = use_device(g)) return r;
+  const size_t n = (size_t)g->nx * g->ny;
+  if (int r = ensure_scratch(g, 3 * n)) return r;
+  double* d = g->scratch;
+  CUDA_TRY(cudaMemcpyAsync(d, rho, n * 8, cudaMemcpyHostToDevice, g->stream), "upload rho");
+  CUDA_TRY(cudaMemcpyAsync(d + n, ux, n * 8, cudaMemcpyHostToDevice, g->stream), "upload ux");
+  CUDA_TRY(cudaMemcpyAsync(d + 2 * n, uy, n * 8, cudaMemcpyHostToDevice, g->stream), "upload uy");
+  CUDA_TRY(equilibrium(internal_storage(g->storage), 0, g->nx, g->ny, g->ld, d, d + n, d + 2 * n, 0,
+                       lattice(g, g->iold), g->stream),
+           "equilibrium kernel");
+  CUDA_TRY(cudaStreamSynchronize(g->stream), "equilibrium sync");
+  return ok();
+}
+
+namespace {
+
+// One fused step from lattice a to lattice b with the handle's settings.
+cudaError_t fused_step(plbm_grid_t* g, const void* a, void* b, const CollParams& p) {
+  Sweep s{g->nx, g->ny, g->ld, a, b, g->stream};
+  if (g->storage != PLBM_F64) return step_pull_dev(g->storage, g->kind, s, p);
+  if (g->kind == PLBM_BGKI && g->ld != g->ny) {
+    // The (ny,nx,0:8) dummy of collide_bgk_improved does not coincide with the
+    // padded lattice: keep the two reference passes.
+    cudaError_t e = fma::stream_f64(s);
+    if (e != cudaSuccess) return e;
+    return g->math == PLBM_MATH_STRICT ? strict::collide_f64(g->kind, s, p) : fma::collide_f64(g->kind, s, p);
+  }
+  switch (g->math) {
+    case PLBM_MATH_STRICT: return strict::step_pull_f64(g->kind, s, p);
+    case PLBM_MATH_DF64: return step_pull_df64(g->kind, s, p);
+    default: return fma::step_pull_f64(g->kind, s, p);
+  }
+}
+
+}  // namespace
+
+extern "C" int plbm_stream(plbm_grid_t* g) {
+  if (int r = check_grid(g)) return r;
+  if (int r = use_device(g)) return r;
+  Sweep s{g->nx, g->ny, g->ld, lattice(g, g->iold), lattice(g, g->inew), g->stream};
+  cudaError_t e = g->storage == PLBM_F64 ? fma::stream_f64(s) : stream_dev(g->storage, s);
+  if (e != cudaSuccess) return cuda_fail(e, "lbm_stream kernel");
+  return ok();
+}
+
+extern "C" int plbm_collide(plbm_grid_t* g) {
+  if (int r = check_grid(g)) return r;
+  if (int r = use_device(g)) return r;
+  const CollParams p = plbm_make_params(g->omega, g->trt_magic);
+  Sweep s{g->nx, g->ny, g->ld, nullptr, lattice(g, g->inew), g->stream};
+  cudaError_t e;
+  if (g->storage != PLBM_F64) e = collide_dev(g->storage, g->kind, s, p);
+  else if (g->math == PLBM_MATH_STRICT) e = strict::collide_f64(g->kind, s, p);
+  else e = fma::collide_f64(g->kind, s, p);
+  if (e != cudaSuccess) return cuda_fail(e, "collision kernel");
+  return ok();
+}
+
+extern "C" int plbm_perform_lbm_step(plbm_grid_t* g, int nsteps) {
+  if (int r = check_grid(g)) return r;
+  if (nsteps < 0) return fail(PLBM_E_INVALID, "nsteps = %d < 0", nsteps);
+  if (g->math == PLBM_MATH_DF64 && g->storage == PLBM_F64 && g->kind == PLBM_BGKI)
+    return fail(PLBM_E_UNSUPPORTED, "PLBM_MATH_DF64 is not offered for collide_bgk_improved");
+  if (int r = use_device(g)) return r;
+  const CollParams p = plbm_make_params(g->omega, g->trt_magic);
+  for (int i = 0; i < nsteps; i++) {
+    cudaError_t e = fused_step(g, lattice(g, g->iold), lattice(g, g->inew), p);
+    if (e != cudaSuccess) return cuda_fail(e, "stream-collide kernel");
+    const int t = g->iold;  // src/periodic_lbm.f90:22-27
+    g->iold = g->inew;
+    g->inew = t;
+  }
+  return ok();
+}
+
+extern "C" int plbm_macros_device(plbm_grid_t* g, int ibuf, double* rho, double* ux, double* uy) {
+  if (int r = check_grid(g)) return r;
+  if (int r = check_buf(g, ibuf)) return r;
+  if (int r = use_device(g)) return r;
+  CUDA_TRY(macros(internal_storage(g->storage), 0, g->nx, g->ny, g->ld, lattice(g, ibuf), rho, ux, uy, g->stream),
+           "moments kernel");
+  return ok();
+}
+
+extern "C" int plbm_update_macros(plbm_grid_t* g, double* rho, double* ux, double* uy) {
+  if (int r = check_grid(g)) return r;
+  if (int r = use_device(g)) return r;
+  const size_t n = (size_t)g->nx * g->ny;
+  if (int r = ensure_scratch(g, 3 * n)) return r;
+  double* d = g->scratch;
+  // src/fvm_bardow.F90:350-352 reads f(:,:,:,grid%inew)
+  CUDA_TRY(macros(internal_storage(g->storage), 0, g->nx, g->ny, g->ld, lattice(g, g->inew), d, d + n, d + 2 * n,
+                  g->stream),
+           "moments kernel");
+  if (rho) CUDA_TRY(cudaMemcpyAsync(rho, d, n * 8, cudaMemcpyDeviceToHost, g->stream), "download rho");
+  if (ux) CUDA_TRY(cudaMemcpyAsync(ux, d + n, n * 8, cudaMemcpyDeviceToHost, g->stream), "download ux");
+  if (uy) CUDA_TRY(cudaMemcpyAsync(uy, d + 2 * n, n * 8, cudaMemcpyDeviceToHost, g->stream), "download uy");
+  CUDA_TRY(cudaStreamSynchronize(g->stream), "update_macros sync");
+  return ok();
+}
+
+extern "C" int plbm_vorticity_device(int order, int nx, int ny, const double* ux, const double* uy, double* w,
+                                     void* stream) {
+  if (nx < 1 || ny < 1) return fail(PLBM_E_INVALID, "grid size %dx%d", nx, ny);
+  if (order != 2 && order != 4 && order != 44) return fail(PLBM_E_INVALID, "vorticity order %d (2, 4 or 44)", order);
+  if (!ux || !uy || !w) return fail(PLBM_E_INVALID, "NULL field");
+  CUDA_TRY(vorticity(order, nx, ny, ux, uy, w, static_cast<cudaStream_t>(stream)), "vorticity kernel");
+  return ok();
+}
+
+extern "C" int plbm_vorticity(int order, int nx, int ny, const double* ux, const double* uy, double* w) {
+  if (nx < 1 || ny < 1) return fail(PLBM_E_INVALID, "grid size %dx%d", nx, ny);
+  if (order != 2 && order != 4 && order != 44) return fail(PLBM_E_INVALID, "vorticity order %d (2, 4 or 44)", order);
+  if (!ux || !uy || !w) return fail(PLBM_E_INVALID, "NULL field");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+    cudaGetLastError();
+    return fail(PLBM_E_NODEVICE, "no CUDA device visible");
+  }
+  const size_t n = (size_t)nx * ny;
+  double* d = nullptr;
+  CUDA_TRY(cudaMalloc(&d, 3 * n * sizeof(double)), "cudaMalloc(vorticity)");
+  cudaError_t e = cudaMemcpy(d, ux, n * 8, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(d + n, uy, n * 8, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = vorticity(order, nx, ny, d, d + n, d + 2 * n, 0);
+  if (e == cudaSuccess) e = cudaMemcpy(w, d + 2 * n, n * 8, cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) return cuda_fail(e, "vorticity");
+  return ok();
+}
+
+namespace {
+int reduce(plbm_grid_t* g, int ibuf, const double* uxa, const double* uya, double out[3]) {
+  const size_t n = (size_t)g->nx * g->ny;
+  const int nb = reduce_blocks(g->nx, g->ny);
+  if (int r = ensure_scratch(g, 3 * n + 3 * (size_t)nb)) return r;
+  double* part = g->scratch + 3 * n;
+  const double* dua = nullptr;
+  const double* dva = nullptr;
+  if (uxa) {
+    CUDA_TRY(cudaMemcpyAsync(g->scratch, uxa, n * 8, cudaMemcpyHostToDevice, g->stream), "upload uxa");
+    CUDA_TRY(cudaMemcpyAsync(g->scratch + n, uya, n * 8, cudaMemcpyHostToDevice, g->stream), "upload uya");
+    dua = g->scratch;
+    dva = g->scratch + n;
+  }
+  CUDA_TRY(energy_error_partials(internal_storage(g->storage), 0, g->nx, g->ny, g->ld, lattice(g, ibuf), dua, dva,
+                                 part, g->stream),
+           "reduction kernel");
+  std::vector<double> h(3 * (size_t)nb);
+  CUDA_TRY(cudaMemcpyAsync(h.data(), part, h.size() * 8, cudaMemcpyDeviceToHost, g->stream), "download partials");
+  CUDA_TRY(cudaStreamSynchronize(g->stream), "reduction sync");
+  out[0] = out[1] = out[2] = 0.0;
+  for (int b = 0; b < nb; b++)
+    for (int k = 0; k < 3; k++) out[k] += h[3 * (size_t)b + k];
+  return PLBM_OK;
+}
+}  // namespace
+
+extern "C" int plbm_kinetic_energy(plbm_grid_t* g, int ibuf, double* energy) {
+  if (int r = check_grid(g)) return r;
+  if (int r = check_buf(g, ibuf)) return r;
+  if (!energy) return fail(PLBM_E_INVALID, "energy is NULL");
+  if (int r = use_device(g)) return r;
+  double s[3];
+  if (int r = reduce(g, ibuf, nullptr, nullptr, s)) return r;
+  *energy = s[0];
+  return ok();
+}
+
+extern "C" int plbm_velocity_l2_error(plbm_grid_t* g, int ibuf, const double* uxa, const double* uya,
+                                      double* err) {
+  if (int r = check_grid(g)) return r;
+  if (int r = check_buf(g, ibuf)) return r;
+  if (!uxa || !uya || !err) return fail(PLBM_E_INVALID, "NULL argument");
+  if (int r = use_device(g)) return r;
+  double s[3];
+  if (int r = reduce(g, ibuf, uxa, uya, s)) return r;
+  if (!(s[2] > 0.0)) return fail(PLBM_E_INVALID, "reference field has zero norm");
+  *err = sqrt(s[1] / s[2]);
+  return ok();
+}
+
+extern "C" int plbm_synchronize(plbm_grid_t* g) {
+  if (int r = check_grid(g)) return r;
+  if (int r = use_device(g)) return r;
+  CUDA_TRY(cudaStreamSynchronize(g->stream), "synchronize");
+  return ok();
+}
+
+extern "C" int plbm_launch_step(int storage, int math, int kind, int nx, int ny, int ld, const void* fsrc,
+                                void* fdst, double omega, double trt_magic, void* stream) {
+  if (nx < 1 || ny < 1 || ld < ny) return fail(PLBM_E_INVALID, "bad sizes nx=%d ny=%d ld=%d", nx, ny, ld);
+  if (!fsrc || !fdst || fsrc == fdst) return fail(PLBM_E_INVALID, "fsrc and fdst must be distinct device lattices");
+  if (kind < PLBM_BGK || kind > PLBM_BGKI) return fail(PLBM_E_INVALID, "unknown collision kind %d", kind);
+  const CollParams p = plbm_make_params(omega, trt_magic);
+  Sweep s{nx, ny, ld, fsrc, fdst, static_cast<cudaStream_t>(stream)};
+  cudaError_t e;
+  if (storage == PLBM_F64) {
+    if (kind == PLBM_BGKI && ld != ny)
+      return fail(PLBM_E_UNSUPPORTED, "fused collide_bgk_improved needs ld == ny");
+    if (math == PLBM_MATH_STRICT) e = strict::step_pull_f64(kind, s, p);
+    else if (math == PLBM_MATH_DF64) e = step_pull_df64(kind, s, p);
+    else e = fma::step_pull_f64(kind, s, p);
+  } else if (storage == PLBM_F32DEV || storage == PLBM_F16DEV) {
+    if (kind == PLBM_BGKI) return fail(PLBM_E_UNSUPPORTED, "collide_bgk_improved needs PLBM_F64 storage");
+    e = step_pull_dev(storage, kind, s, p);
+  } else {
+    return fail(PLBM_E_INVALID, "unknown storage %d", storage);
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "stream-collide kernel");
+  return ok();
+}

@@ -1,0 +1,74 @@
+// plbm_launch.h -- internal launcher interface shared by the translation units
+// of libplbmgpu.so.  Not part of the public C ABI.
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include "plbm_device.cuh"
+
+namespace plbm {
+
+// One lattice sweep: nx, ny, ld and the two lattices.
+struct Sweep {
+  int nx, ny, ld;
+  const void* src;
+  void* dst;
+  cudaStream_t stream;
+};
+
+// Threads per block of the per-cell kernels.
+constexpr int kBlock = 256;
+
+// The binary64 reference kernels exist twice, once compiled with FMA
+// contraction (namespace fma) and once without (namespace strict).
+#define PLBM_DECLARE_F64(NS)                                                              \
+  namespace NS {                                                                          \
+  /* fused lbm_stream + collide_* (src/periodic_lbm.f90:15-29), YFast layout */            \
+  cudaError_t step_pull_f64(int kind, const Sweep& s, const CollParams& p);               \
+  /* lbm_stream alone (src/periodic_lbm.f90:45-127) */                                   \
+  cudaError_t stream_f64(const Sweep& s);                                                 \
+  /* collide_* alone, in place on s.dst (s.src ignored) */                                \
+  cudaError_t collide_f64(int kind, const Sweep& s, const CollParams& p);                 \
+  /* plugin step: shifted binary64 collide + push (sim/sim.F90:404-505), XFast */          \
+  cudaError_t step_push_shift_f64(int kind, const Sweep& s, const CollParams& p);         \
+  }
+PLBM_DECLARE_F64(fma)
+PLBM_DECLARE_F64(strict)
+#undef PLBM_DECLARE_F64
+
+// binary64 storage, double-float arithmetic (YFast pull)
+cudaError_t step_pull_df64(int kind, const Sweep& s, const CollParams& p);
+
+// Deviation storage (storage = 1 float, 2 half), binary32 arithmetic.
+cudaError_t step_pull_dev(int storage, int kind, const Sweep& s, const CollParams& p);
+cudaError_t stream_dev(int storage, const Sweep& s);
+cudaError_t collide_dev(int storage, int kind, const Sweep& s, const CollParams& p);
+cudaError_t step_push_dev(int storage, int kind, const Sweep& s, const CollParams& p);
+
+// Field kernels (fields.cu).  layout: 0 = YFast (src/), 1 = XFast (sim/).
+// storage 0 = binary64 f (unshifted), 3 = binary64 shifted, 1/2 = deviation.
+enum { ST_F64 = 0, ST_F32DEV = 1, ST_F16DEV = 2, ST_F64SHIFT = 3 };
+// Moments of one lattice into (fast,slow) arrays; reference order of
+// update_macros (YFast, unshifted) or lbm_macros (shifted).
+cudaError_t macros(int storage, int layout, int nx, int ny, int ld, const void* f, double* rho,
+                   double* ux, double* uy, cudaStream_t st);
+// Equilibrium from (fast,slow) rho/ux/uy arrays into a lattice.
+//   storage 0: equilibrium() of src/fvm_bardow.F90:99-126;
+//   storage 3/1/2: shifted equilibrium of sim/sim.F90:353-401 with rho = 1 + p/cs^2
+//   when from_pressure != 0.
+cudaError_t equilibrium(int storage, int layout, int nx, int ny, int ld, const double* rho,
+                        const double* ux, const double* uy, int from_pressure, void* f,
+                        cudaStream_t st);
+// binary64 f (YFast) <-> deviation storage conversion: h = f - w_i.
+cudaError_t f64_to_dev(int storage, int nx, int ny, int ld, const double* f, void* h, cudaStream_t st);
+cudaError_t dev_to_f64(int storage, int nx, int ny, int ld, const void* h, double* f, cudaStream_t st);
+// Vorticity on (ny,nx) device arrays.
+cudaError_t vorticity(int order, int nx, int ny, const double* ux, const double* uy, double* w,
+                      cudaStream_t st);
+// Per-block binary64 partial sums of 0.5*rho*|u|^2 and of |u-ua|^2, |ua|^2
+// over the moments of a lattice; partial has room for reduce_blocks() triples.
+int reduce_blocks(int nx, int ny);
+cudaError_t energy_error_partials(int storage, int layout, int nx, int ny, int ld, const void* f,
+                                  const double* uxa, const double* uya, double* partial,
+                                  cudaStream_t st);
+
+}  // namespace plbm

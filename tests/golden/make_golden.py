@@ -1,0 +1,333 @@
+"""Generate the golden fixtures in tests/golden/*.npz.
+
+The reference (Fortran, ivan-pi/periodic-lbm) ships no golden vectors and no
+Fortran compiler is available, so the fixtures come from a SECOND restatement
+of the Fortran written here in vectorised numpy, independently of the C
+oracle (oracle/plbm_oracle.c): streaming by array rolls, collisions as whole-
+array expressions in the Fortran association.  tests/test_oracle.py checks the
+C oracle against these fixtures bit for bit, so two separate readings of the
+Fortran agree.  Inputs are seeded.
+
+    python tests/golden/make_golden.py      # rewrites tests/golden/golden.npz
+"""
+from __future__ import annotations
+
+import math
+from pathlib import Path
+
+import numpy as np
+
+OUT = Path(__file__).resolve().parent / "golden.npz"
+
+W0, WS, WD = 4.0 / 9.0, 1.0 / 9.0, 1.0 / 36.0
+CSQR = 1.0 / 3.0
+CX = [0, 1, 0, -1, 0, 1, -1, -1, 1]
+CY = [0, 0, 1, 0, -1, 1, 1, -1, -1]
+W = [W0, WS, WS, WS, WS, WD, WD, WD, WD]
+
+
+def pad16(n):
+    return n + (16 - n % 16) % 16
+
+
+# --- src/periodic_lbm.f90:45-127: fdst(y,x,q) = fsrc(y-cy, x-cx, q) on rows 1:ny
+def stream(f, ny):
+    g = f.copy()
+    for q in range(9):
+        g[q, :, :ny] = np.roll(f[q, :, :ny], shift=(CX[q], CY[q]), axis=(0, 1))
+    return g
+
+
+# --- src/fvm_bardow.F90:99-126
+def equilibrium(rho, ux, uy):
+    uxx = ux * ux
+    uyy = uy * uy
+    indp = 1.0 - 1.5 * (uxx + uyy)
+    feq = [None] * 9
+    feq[0] = W0 * rho * (indp)
+    feq[1] = WS * rho * (indp + 3.0 * ux + 4.5 * uxx)
+    feq[2] = WS * rho * (indp + 3.0 * uy + 4.5 * uyy)
+    feq[3] = WS * rho * (indp - 3.0 * ux + 4.5 * uxx)
+    feq[4] = WS * rho * (indp - 3.0 * uy + 4.5 * uyy)
+    uxpy = ux + uy
+    feq[5] = WD * rho * (indp + 3.0 * uxpy + 4.5 * uxpy * uxpy)
+    feq[7] = WD * rho * (indp - 3.0 * uxpy + 4.5 * uxpy * uxpy)
+    uxmy = ux - uy
+    feq[6] = WD * rho * (indp - 3.0 * uxmy + 4.5 * uxmy * uxmy)
+    feq[8] = WD * rho * (indp + 3.0 * uxmy + 4.5 * uxmy * uxmy)
+    return feq
+
+
+# --- src/collision_bgk.F90:58-71
+def bgk(f, ny, omega):
+    fs = [f[q, :, :ny] for q in range(9)]
+    rho = (((fs[5] + fs[7]) + (fs[6] + fs[8])) + ((fs[1] + fs[3]) + (fs[2] + fs[4]))) + fs[0]
+    invrho = 1.0 / rho
+    ux = invrho * (((fs[5] - fs[7]) + (fs[8] - fs[6])) + (fs[1] - fs[3]))
+    uy = invrho * (((fs[5] - fs[7]) + (fs[6] - fs[8])) + (fs[2] - fs[4]))
+    feq = equilibrium(rho, ux, uy)
+    ob = 1.0 - omega
+    out = f.copy()
+    for q in range(9):
+        out[q, :, :ny] = ob * fs[q] + omega * feq[q]
+    return out
+
+
+# --- src/collision_trt.F90:12-34,64-160
+T0 = 4.0 / 9.0
+T1X2 = (1.0 / 9.0) * 2.0
+T2X2 = (1.0 / 36.0) * 2.0
+INV2CSQ2 = 1.0 / (2.0 * (1.0 / 3.0) * (1.0 / 3.0))
+FAC1 = T1X2 * INV2CSQ2
+FAC2 = T2X2 * INV2CSQ2
+
+
+def lambda_d(omega, x):
+    return (4.0 - 2.0 * omega) / (4.0 * x * omega + 2.0 - omega)
+
+
+def trt(f, ny, le, ld):
+    vC, vE, vN, vW, vS, vNE, vNW, vSW, vSE = [f[q, :, :ny] for q in range(9)]
+    les, lds = 0.5 * le, 0.5 * ld
+    rho = (((vNE + vSW) + (vNW + vSE)) + ((vE + vW) + (vN + vS))) + vC
+    velX = (((vNE - vSW) + (vSE - vNW)) + (vE - vW))
+    velY = (((vNE - vSW) + (vNW - vSE)) + (vN - vS))
+    velX2, velY2 = velX * velX, velY * velY
+    fc = rho - 1.5 * (velX2 + velY2)
+    out = f.copy()
+    o = lambda q, v: out.__setitem__((q, slice(None), slice(0, ny)), v)  # noqa: E731
+    o(0, vC * (1.0 - le) + le * T0 * fc)
+    xpy = velX + velY
+    sym = les * (vNE + vSW - FAC2 * xpy * xpy - T2X2 * fc)
+    asym = lds * (vNE - vSW - 3.0 * T2X2 * xpy)
+    o(5, vNE - sym - asym)
+    o(7, vSW - sym + asym)
+    xmy = velX - velY
+    sym = les * (vSE + vNW - FAC2 * xmy * xmy - T2X2 * fc)
+    asym = lds * (vSE - vNW - 3.0 * T2X2 * xmy)
+    o(8, vSE - sym - asym)
+    o(6, vNW - sym + asym)
+    sym = les * (vN + vS - FAC1 * velY2 - T1X2 * fc)
+    asym = lds * (vN - vS - 3.0 * T1X2 * velY)
+    o(2, vN - sym - asym)
+    o(4, vS - sym + asym)
+    sym = les * (vE + vW - FAC1 * velX2 - T1X2 * fc)
+    asym = lds * (vE - vW - 3.0 * T1X2 * velX)
+    o(1, vE - sym - asym)
+    o(3, vW - sym + asym)
+    return out
+
+
+# --- src/collision_regularized.F90:63-194
+def rr(f, ny, omega):
+    vC, vE, vN, vW, vS, vNE, vNW, vSW, vSE = [f[q, :, :ny].copy() for q in range(9)]
+    rho = (((vNE + vSW) + (vNW + vSE)) + ((vE + vW) + (vN + vS))) + vC
+    invrho = 1.0 / rho
+    ux = invrho * (((vNE - vSW) + (vSE - vNW)) + (vE - vW))
+    uy = invrho * (((vNE - vSW) + (vNW - vSE)) + (vN - vS))
+    uxx, uyy = ux * ux, uy * uy
+    uxxy, uyyx, uxxyy = uxx * uy, uyy * ux, uxx * uyy
+    indp0 = 1.0 - 1.5 * (uxx + uyy)
+    indps = indp0 - 4.5 * uxxyy
+    indpd = indp0 + 9.0 * uxxyy
+    indp0 = indp0 + 2.25 * uxxyy
+    feq = [None] * 9
+    feq[0] = W0 * rho * indp0
+    feq[1] = WS * rho * (indps + 3.0 * ux + 4.5 * (uxx - uyyx))
+    feq[3] = WS * rho * (indps - 3.0 * ux + 4.5 * (uxx + uyyx))
+    feq[2] = WS * rho * (indps + 3.0 * uy + 4.5 * (uyy - uxxy))
+    feq[4] = WS * rho * (indps - 3.0 * uy + 4.5 * (uyy + uxxy))
+    vC, vE, vN, vW, vS = vC - feq[0], vE - feq[1], vN - feq[2], vW - feq[3], vS - feq[4]
+    axx = CSQR * (2.0 * (vE + vW) - (vN + vS) - vC)
+    ayy = CSQR * (2.0 * (vN + vS) - (vE + vW) - vC)
+    u3p, uxpy = uxxy + uyyx, ux + uy
+    indp57 = indpd + 4.5 * uxpy * uxpy
+    feq[5] = WD * rho * (indp57 + 3.0 * uxpy + 9.0 * u3p)
+    feq[7] = WD * rho * (indp57 - 3.0 * uxpy - 9.0 * u3p)
+    u3m, uxmy = uxxy - uyyx, ux - uy
+    indp68 = indpd + 4.5 * uxmy * uxmy
+    feq[6] = WD * rho * (indp68 - 3.0 * uxmy + 9.0 * u3m)
+    feq[8] = WD * rho * (indp68 + 3.0 * uxmy - 9.0 * u3m)
+    vNE, vNW, vSW, vSE = vNE - feq[5], vNW - feq[6], vSW - feq[7], vSE - feq[8]
+    tmp = 2.0 * CSQR * (vNE + vNW + vSW + vSE)
+    axx, ayy = axx + tmp, ayy + tmp
+    axy = ((vNE + vSW) - (vNW + vSE))
+    axxy = 2.0 * ux * axy + uy * axx
+    ayyx = 2.0 * uy * axy + ux * ayy
+    axxyy = 2.0 * (ux * ayyx + uy * axxy) - uxx * ayy - uyy * axx - 4.0 * ux * uy * axy
+    i0 = -1.5 * (axx + ayy)
+    i_s = i0 - 4.5 * axxyy
+    i_d = 9.0 * axxyy - 2.0 * i0
+    i0 = i0 + 2.25 * axxyy
+    a = [i0, i_s + 4.5 * (axx - ayyx), i_s + 4.5 * (ayy - axxy), i_s + 4.5 * (axx + ayyx),
+         i_s + 4.5 * (ayy + axxy), i_d + 9.0 * (axxy + ayyx + axy), i_d + 9.0 * (axxy - ayyx - axy),
+         i_d - 9.0 * (axxy + ayyx - axy), i_d - 9.0 * (axxy - ayyx + axy)]
+    wts = [W0 * (1.0 - omega), WS * (1.0 - omega), WD * (1.0 - omega)]
+    out = f.copy()
+    for q in range(9):
+        wq = wts[0] if q == 0 else (wts[1] if q < 5 else wts[2])
+        out[q, :, :ny] = feq[q] + wq * a[q]
+    return out
+
+
+# --- src/collision_bgk_improved.f90:24-107, on the (ny,nx,0:8) dummy view
+def bgki(f, nx, ny, omega):
+    flat = f.reshape(-1).copy()
+    n = nx * ny
+    v = [flat[q * n:(q + 1) * n].copy() for q in range(9)]
+    vC, vE, vN, vW, vS, vNE, vNW, vSW, vSE = v
+    fac = 4.5 - 2.25 * omega
+    ob = 1.0 - omega
+    rho = (((vNE + vSW) + (vNW + vSE)) + ((vE + vW) + (vN + vS))) + vC
+    invrho = 1.0 / rho
+    sX1, sXN = vE + vNE + vSE, vW + vNW + vSW
+    sY1, sYN = vN + vNE + vNW, vS + vSE + vSW
+    m10, m01 = invrho * (sX1 - sXN), invrho * (sY1 - sYN)
+    u2, v2 = m10 * m10, m01 * m01
+    m20, m02 = invrho * (sX1 + sXN), invrho * (sY1 + sYN)
+    Gx = fac * u2 * (m20 - 1.0 / 3.0 - u2)
+    Gy = fac * v2 * (m02 - 1.0 / 3.0 - v2)
+    X0 = -2.0 / 3.0 + u2 + Gx
+    X1 = -(X0 + 1.0 + m10) * 0.5
+    XN = X1 + m10
+    Y0 = -2.0 / 3.0 + v2 + Gy
+    Y1 = -(Y0 + 1.0 + m01) * 0.5
+    YN = Y1 + m01
+    ro = rho * omega
+    X0, X1, XN = X0 * ro, X1 * ro, XN * ro
+    new = [ob * vC + X0 * Y0, ob * vE + X1 * Y0, ob * vN + X0 * Y1, ob * vW + XN * Y0, ob * vS + X0 * YN,
+           ob * vNE + X1 * Y1, ob * vNW + XN * Y1, ob * vSW + XN * YN, ob * vSE + X1 * YN]
+    for q in range(9):
+        flat[q * n:(q + 1) * n] = new[q]
+    return flat.reshape(f.shape)
+
+
+# --- src/fvm_bardow.F90:356-388
+def macros(f, ny):
+    fs = [f[q, :, :ny] for q in range(9)]
+    rho = fs[0] + (((fs[5] + fs[7]) + (fs[6] + fs[8])) + ((fs[1] + fs[3]) + (fs[2] + fs[4])))
+    invrho = 1.0 / rho
+    ux = invrho * (((fs[5] - fs[7]) + (fs[8] - fs[6])) + (fs[1] - fs[3]))
+    uy = invrho * (((fs[5] - fs[7]) + (fs[6] - fs[8])) + (fs[2] - fs[4]))
+    return rho, ux, uy
+
+
+# --- src/vorticity.f90 on (nx, ny) arrays a[x, y]
+def vort2(ux, uy):
+    duydx = 0.5 * (np.roll(uy, -1, 0) - np.roll(uy, 1, 0))
+    duxdy = 0.5 * (np.roll(ux, -1, 1) - np.roll(ux, 1, 1))
+    return duydx - duxdy
+
+
+def vort4(ux, uy):
+    t1, t2 = 1.0 / 12.0, 2.0 / 3.0
+    duydx = t1 * (np.roll(uy, -1, 0) - np.roll(uy, 1, 0)) + t2 * (np.roll(uy, 2, 0) - np.roll(uy, -2, 0))
+    duxdy = t1 * (np.roll(ux, -1, 1) - np.roll(ux, 1, 1)) + t2 * (np.roll(ux, 2, 1) - np.roll(ux, -2, 1))
+    return duydx - duxdy
+
+
+# --- sim/sim.F90 plugin semantics on bulk arrays (9, ny, nx), x fastest
+def sim_eq(rho, ux, uy):
+    uxx, uyy = ux * ux, uy * uy
+    uxpy, uxmy = ux + uy, ux - uy
+    indp = -1.5 * (uxx + uyy)
+    feq = [W0 * rho * (indp), WS * rho * (indp + 3.0 * ux + 4.5 * uxx), WS * rho * (indp + 3.0 * uy + 4.5 * uyy),
+           WS * rho * (indp - 3.0 * ux + 4.5 * uxx), WS * rho * (indp - 3.0 * uy + 4.5 * uyy),
+           WD * rho * (indp + 3.0 * uxpy + 4.5 * uxpy * uxpy), WD * rho * (indp - 3.0 * uxmy + 4.5 * uxmy * uxmy),
+           WD * rho * (indp - 3.0 * uxpy + 4.5 * uxpy * uxpy), WD * rho * (indp + 3.0 * uxmy + 4.5 * uxmy * uxmy)]
+    return [feq[q] + W[q] * (rho - 1.0) for q in range(9)]
+
+
+def sim_step(h, omega):
+    fs = [h[q] for q in range(9)]
+    rho = (((fs[5] + fs[7]) + (fs[6] + fs[8])) + ((fs[1] + fs[3]) + (fs[2] + fs[4]))) + fs[0]
+    rho = rho + 1.0
+    ux = (((fs[5] - fs[7]) + (fs[8] - fs[6])) + (fs[1] - fs[3])) / rho
+    uy = (((fs[5] - fs[7]) + (fs[6] - fs[8])) + (fs[2] - fs[4])) / rho
+    feq = sim_eq(rho, ux, uy)
+    out = np.empty_like(h)
+    for q in range(9):
+        post = omega * (feq[q] - fs[q]) + fs[q]
+        out[q] = np.roll(post, shift=(CY[q], CX[q]), axis=(0, 1))
+    return out
+
+
+def sim_macros(h):
+    fs = [h[q] for q in range(9)]
+    rho = (((fs[5] + fs[7]) + (fs[6] + fs[8])) + ((fs[1] + fs[3]) + (fs[2] + fs[4]))) + fs[0] + 1.0
+    u = (((fs[5] - fs[7]) + (fs[8] - fs[6])) + (fs[1] - fs[3])) / rho
+    v = (((fs[5] - fs[7]) + (fs[6] - fs[8])) + (fs[2] - fs[4])) / rho
+    return rho, u, v
+
+
+def perturbed_equilibrium(nx, ny, rng, amp=1e-3, noise=1e-5):
+    ld = pad16(ny)
+    k = 2 * math.pi
+    xx = (np.arange(nx) + 0.5)[:, None] / nx
+    yy = (np.arange(ny) + 0.5)[None, :] / ny
+    ux = amp * 30 * np.sin(k * yy) * np.cos(k * xx) + noise * rng.standard_normal((nx, ny))
+    uy = -amp * 20 * np.cos(k * yy) * np.sin(k * xx) + noise * rng.standard_normal((nx, ny))
+    rho = 1.0 + amp * rng.standard_normal((nx, ny))
+    f = np.zeros((9, nx, ld))
+    feq = equilibrium(rho, ux, uy)
+    for q in range(9):
+        f[q, :, :ny] = feq[q] * (1.0 + noise * 10 * rng.standard_normal((nx, ny)))
+    return rho, ux, uy, f
+
+
+def main():
+    rng = np.random.default_rng(20240501)
+    g = {}
+    # lattice cases: (nx, ny) with ld != ny and ld == ny
+    for nx, ny in [(17, 13), (12, 32)]:
+        tag = f"{nx}x{ny}"
+        rho, ux, uy, f0 = perturbed_equilibrium(nx, ny, rng)
+        g[f"{tag}_f0"] = f0
+        g[f"{tag}_eq_rho"], g[f"{tag}_eq_ux"], g[f"{tag}_eq_uy"] = rho, ux, uy
+        feq = equilibrium(rho, ux, uy)
+        fe = np.zeros_like(f0)
+        for q in range(9):
+            fe[q, :, :ny] = feq[q]
+        g[f"{tag}_equilibrium"] = fe
+        g[f"{tag}_stream"] = stream(f0, ny)
+        g[f"{tag}_macros"] = np.stack(macros(f0, ny))
+        for kind, omega in [("bgk", 1.25), ("trt", 1.6), ("rr", 1.9)]:
+            f = f0.copy()
+            for _ in range(10):
+                f = stream(f, ny)
+                if kind == "bgk":
+                    f = bgk(f, ny, omega)
+                elif kind == "trt":
+                    f = trt(f, ny, omega, lambda_d(omega, 0.25))
+                else:
+                    f = rr(f, ny, omega)
+            g[f"{tag}_{kind}_10"] = f
+        g[f"{tag}_bgki_collide"] = bgki(f0, nx, ny, 1.3)
+        w2 = vort2(ux, uy)
+        w4 = vort4(ux, uy)
+        g[f"{tag}_vort2"], g[f"{tag}_vort4"] = w2, w4
+    # plugin (sim/) semantics on a 13 x 11 grid
+    nx, ny = 13, 11
+    k = 2 * math.pi / nx
+    xx = (np.arange(nx) + 0.5)[None, :]
+    yy = (np.arange(ny) + 0.5)[:, None]
+    u = -0.02 * np.cos(k * xx) * np.sin(k * yy) + 1e-4 * rng.standard_normal((ny, nx))
+    v = 0.02 * np.sin(k * xx) * np.cos(k * yy) + 1e-4 * rng.standard_normal((ny, nx))
+    p = -0.25 * 0.02 ** 2 * (np.cos(2 * k * xx) + np.cos(2 * k * yy)) * np.ones((ny, nx))
+    g["sim_p"], g["sim_u"], g["sim_v"] = p, u, v
+    h = np.stack(sim_eq(1.0 + p / CSQR, u, v))
+    g["sim_h0"] = h
+    for _ in range(10):
+        h = sim_step(h, 1.7)
+    g["sim_h10"] = h
+    g["sim_macros10"] = np.stack(sim_macros(h))
+    # scalar properties (src/fvm_bardow.F90:242-269)
+    nu = 0.1 / 3.0
+    tau = 3.0 * nu
+    g["props"] = np.array([tau, 1.0 / (tau + 0.5 * 1.0), (tau / 1.0) ** 2, lambda_d(1.25, 0.25)])
+    np.savez_compressed(OUT, **g)
+    print(f"wrote {OUT} ({OUT.stat().st_size} bytes, {len(g)} arrays)")
+
+
+if __name__ == "__main__":
+    main()

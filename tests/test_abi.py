@@ -1,0 +1,126 @@
+"""CPU tests of the C ABI library: it builds, loads, exports every declared
+entry point, and rejects bad arguments before touching a device."""
+import ctypes as C
+import re
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+@pytest.fixture(scope="module")
+def lib():
+    import __graft_entry__ as ge
+    ge.build()
+    from plbm import _lib
+    return _lib.load()
+
+
+def declared_functions():
+    names = []
+    for h in sorted((ROOT / "include").glob("*.h")):
+        text = h.read_text()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"^[A-Za-z_][\w\s\*]*?\b((?:plbm|c_plbmgpu)_\w+)\s*\(", text, flags=re.M):
+            names.append(m.group(1))
+    return sorted(set(names))
+
+
+def test_headers_declare_the_abi():
+    names = declared_functions()
+    for must in ("plbm_grid_create", "plbm_perform_lbm_step", "plbm_update_macros", "plbm_vorticity",
+                 "c_plbmgpu_init", "c_plbmgpu_step", "c_plbmgpu_vars", "c_plbmgpu_free", "c_plbmgpu_norm"):
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol(lib):
+    out = subprocess.run(["nm", "-D", "--defined-only", str(ROOT / "periodic-lbm_gb300" / "libplbmgpu.so")],
+                         capture_output=True, text=True, check=True).stdout
+    exported = set(re.findall(r"\sT\s(\w+)$", out, flags=re.M))
+    missing = [n for n in declared_functions() if n not in exported]
+    assert not missing, f"declared but not exported: {missing}"
+    for n in declared_functions():
+        assert getattr(lib, n) is not None
+
+
+def test_python_binding_covers_every_symbol(lib):
+    from plbm import _lib
+    bound = set(_lib.SIGNATURES) | set(_lib.OPTIONAL_SIGNATURES)
+    assert set(declared_functions()) <= bound
+
+
+def test_invalid_arguments_are_rejected_without_a_device(lib):
+    from plbm import _lib
+    h = C.c_void_p()
+    assert lib.plbm_grid_create(0, 8, 2, 0, C.byref(h)) == _lib.PLBM_E_INVALID
+    assert "nx and ny" in _lib.last_error()
+    assert lib.plbm_grid_create(8, 8, 1, 0, C.byref(h)) == _lib.PLBM_E_INVALID
+    assert lib.plbm_grid_create(8, 8, 2, 7, C.byref(h)) == _lib.PLBM_E_INVALID
+    assert lib.plbm_grid_create(8, 8, 2, 0, None) == _lib.PLBM_E_INVALID
+    assert lib.plbm_grid_destroy(None) == _lib.PLBM_OK
+    assert lib.plbm_perform_lbm_step(None, 1) == _lib.PLBM_E_INVALID
+    assert lib.plbm_vorticity(3, 4, 4, None, None, None) == _lib.PLBM_E_INVALID
+    assert lib.plbm_launch_step(0, 0, 0, 8, 8, 4, None, None, 1.0, 0.25, None) == _lib.PLBM_E_INVALID
+
+
+def test_create_without_device_reports_nodevice_or_succeeds(lib):
+    from plbm import _lib
+    h = C.c_void_p()
+    rc = lib.plbm_grid_create(8, 8, 2, 0, C.byref(h))
+    if rc == _lib.PLBM_OK:
+        assert lib.plbm_grid_destroy(h) == _lib.PLBM_OK
+    else:
+        assert rc == _lib.PLBM_E_NODEVICE, _lib.last_error()
+
+
+def test_plugin_init_rejects_reference_error_cases(lib):
+    from plbm import _lib
+    nx, ny = 4, 3
+    p = np.zeros((nx, ny), order="F")
+    u = np.zeros((nx, ny, 2), order="F")
+    # dt /= 1 (sim/sim_slbm.F90:71-74)
+    assert not lib.c_plbmgpu_init(nx, ny, 0.5, p.ctypes.data, u.ctypes.data, None, None)
+    assert "dt = 1.0" in _lib.last_error()
+    # sigma present (sim/sim_slbm.F90:88-93)
+    s = np.zeros((nx, ny, 3), order="F")
+    assert not lib.c_plbmgpu_init(nx, ny, 1.0, p.ctypes.data, u.ctypes.data, s.ctypes.data, None)
+    assert "sigma" in _lib.last_error()
+    assert lib.c_plbmgpu_status(None) == _lib.PLBM_E_INVALID
+
+
+def test_plugin_norm_is_host_arithmetic(lib):
+    rng = np.random.default_rng(0)
+    u = np.asfortranarray(rng.standard_normal((5, 7)))
+    ua = np.asfortranarray(rng.standard_normal((5, 7)))
+    got = lib.c_plbmgpu_norm(5, 7, u.ctypes.data, ua.ctypes.data)
+    ref = np.linalg.norm(u - ua) / np.linalg.norm(ua)
+    assert abs(got - ref) < 1e-14 * ref
+
+
+def test_simplugin_symbol_names_follow_file_stem(lib):
+    from plbm.plugin import SimPlugin
+    sp = SimPlugin()
+    assert sp.c_init.__name__ == "c_plbmgpu_init"
+    with pytest.raises(Exception):
+        sp.init((4, 3), 0.5, np.zeros((4, 3)), np.zeros((4, 3, 2)))
+
+
+def test_cases_match_oracle_initial_conditions():
+    from oracle import oracle as O
+    from plbm import cases
+    p, ux, uy = cases.taylor_green(12, 12, 0.5, 0.5, 0.01, 0.1, t=3.0)
+    q = O.taylor_green(12, 12, 0.5, 0.5, 0.01, 0.1, t=3.0)
+    for a, b in zip((p, ux, uy), q):
+        assert np.max(np.abs(a - b)) <= 1e-17 + 1e-15 * np.max(np.abs(b))
+    r, u, v = cases.shear_layer(10, 14, 14.0, 0.04, 80.0, 0.05)
+    s = O.shear_layer(10, 14, 14.0, 0.04, 80.0, 0.05)
+    for a, b in zip((r, u, v), s):
+        assert np.max(np.abs(a - b)) <= 1e-15 * max(1.0, np.max(np.abs(b)))
+
+
+def test_pad16():
+    from plbm import pad16
+    assert [pad16(n) for n in (1, 15, 16, 17, 32, 33)] == [16, 16, 16, 32, 32, 48]

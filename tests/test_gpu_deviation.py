@@ -1,0 +1,101 @@
+"""GPU tests of deviation storage (h = f - w in binary32 / scaled binary16 with
+binary32 collision): accuracy against the binary64 path, conservation, and
+conversion round trips.  The velocity L2 error bounds below are the stated
+accuracy of these storage forms on the given cases."""
+import math
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def tgv(n, u0=0.05):
+    from plbm import cases
+    k = 2 * math.pi / n
+    p, ux, uy = cases.taylor_green(n, n, k, k, u0, 0.1)
+    return cases.tgv_density(p), ux, uy
+
+
+def run(storage, kind, n, steps, omega=1.25):
+    from plbm import LatticeGrid
+    rho, ux, uy = tgv(n)
+    g = LatticeGrid(n, n, storage=storage, collision=kind)
+    g.set_relaxation(omega, 0.25)
+    g.set_pdf_to_equilibrium(rho, ux, uy)
+    g.perform_lbm_step(steps)
+    out = g.download(g.iold)
+    g.close()
+    return O.update_macros(out, n)
+
+
+def l2(u, v, ur, vr):
+    return math.sqrt(np.sum((u - ur) ** 2 + (v - vr) ** 2) / np.sum(ur ** 2 + vr ** 2))
+
+
+# bounds on the relative velocity L2 error vs binary64 after 400 steps at u0 = 0.05
+BOUND = {"f32dev": 2e-5, "f16dev": 2e-2}
+
+
+@pytest.mark.parametrize("storage", ["f32dev", "f16dev"])
+@pytest.mark.parametrize("kind,omega", [("bgk", 1.25), ("trt", 1.25), ("rr", 1.6)])
+def test_deviation_storage_accuracy(gpu_lib, storage, kind, omega):
+    n, steps = 96, 400
+    r64, u64, v64 = run("f64", kind, n, steps, omega)
+    r, u, v = run(storage, kind, n, steps, omega)
+    err = l2(u, v, u64, v64)
+    print(f"{storage} {kind}: velocity L2 error vs binary64 = {err:.3e}")
+    assert err < BOUND[storage]
+    assert np.max(np.abs(r - r64)) < (1e-6 if storage == "f32dev" else 1e-2)
+
+
+@pytest.mark.parametrize("storage,tol", [("f32dev", 2e-8), ("f16dev", 2e-5)])
+def test_upload_download_round_trip(gpu_lib, storage, tol):
+    from plbm import LatticeGrid
+    n = 40
+    rho, ux, uy = tgv(n)
+    f = O.set_pdf_to_equilibrium(rho, ux, uy)
+    g = LatticeGrid(n, n, storage=storage)
+    g.upload(f, 1)
+    back = g.download(1)
+    g.close()
+    assert np.max(np.abs(back[:, :, :n] - f[:, :, :n])) < tol
+
+
+@pytest.mark.parametrize("storage", ["f32dev", "f16dev"])
+def test_deviation_mass_conservation(gpu_lib, storage):
+    from plbm import LatticeGrid
+    n = 64
+    rho, ux, uy = tgv(n)
+    g = LatticeGrid(n, n, storage=storage)
+    g.set_relaxation(1.5, 0.25)
+    g.set_pdf_to_equilibrium(rho, ux, uy)
+    m0 = O.update_macros(g.download(g.iold), n)[0].sum()
+    g.perform_lbm_step(200)
+    m1 = O.update_macros(g.download(g.iold), n)[0].sum()
+    g.close()
+    assert abs(m1 - m0) / m0 < (1e-6 if storage == "f32dev" else 1e-3)
+
+
+@pytest.mark.parametrize("storage", ["f32dev", "f16dev"])
+def test_plugin_deviation_storage(gpu_lib, storage):
+    from plbm.plugin import SimPlugin, make_params
+    nx, ny = 48, 40
+    x = (np.arange(nx) + 0.5)[:, None]
+    y = (np.arange(ny) + 0.5)[None, :]
+    u = np.empty((nx, ny, 2), order="F")
+    u[:, :, 0] = -0.03 * np.cos(2 * np.pi * x / nx) * np.sin(2 * np.pi * y / ny)
+    u[:, :, 1] = 0.03 * np.sin(2 * np.pi * x / nx) * np.cos(2 * np.pi * y / ny)
+    p = np.zeros((nx, ny), order="F")
+    res = {}
+    for st in ("f64", storage):
+        s = SimPlugin()
+        s.init((nx, ny), 1.0, p, u, params=make_params(storage=st))
+        s.steps(1.4, 300)
+        res[st] = s.vars()
+        s.free()
+    (_, ua), (_, ub) = res["f64"], res[storage]
+    err = np.linalg.norm(ub - ua) / np.linalg.norm(ua)
+    assert err < BOUND[storage]

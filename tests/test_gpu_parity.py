@@ -1,0 +1,251 @@
+"""GPU parity of the binary64 hot path against the oracle, through the C ABI.
+
+Bars:
+* PLBM_MATH_STRICT (no FMA contraction): bit-identical to the oracle, which
+  performs the Fortran's IEEE operations in the Fortran order.
+* PLBM_MATH_FMA (default): norm-wise relative L-infinity error of rho and u
+  <= 1e-12 (the tolerance the hot path is specified to), populations <= 1e-12.
+* integer index work (wrap maps): bit-exact.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-12  # norm-wise relative L-inf, rho and u, binary64 FMA path
+KIND = {"bgk": O.BGK, "trt": O.TRT, "rr": O.RR, "bgki": O.BGKI}
+GRIDS = [(17, 13), (64, 64), (256, 192), (33, 48)]
+
+
+def relinf(a, b):
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def initial_state(nx, ny, seed=11, u0=0.04, noise=1e-4):
+    """Near-equilibrium f with shear, density variation and non-equilibrium noise."""
+    rng = np.random.default_rng(seed)
+    xx = (np.arange(nx) + 0.5)[:, None] / nx
+    yy = (np.arange(ny) + 0.5)[None, :] / ny
+    ux = u0 * np.sin(2 * np.pi * yy) * np.cos(2 * np.pi * xx) + noise * rng.standard_normal((nx, ny))
+    uy = -u0 * np.cos(2 * np.pi * yy) * np.sin(2 * np.pi * xx) + noise * rng.standard_normal((nx, ny))
+    rho = 1.0 + 1e-3 * rng.standard_normal((nx, ny))
+    f = O.set_pdf_to_equilibrium(rho, ux, uy)
+    f[:, :, :ny] *= 1.0 + noise * rng.standard_normal((9, nx, ny))
+    return f
+
+
+def oracle_steps(f0, ny, kind, omega, magic, nsteps):
+    f2 = np.stack([np.zeros_like(f0), f0.copy()])
+    iold, inew = O.perform_lbm_step(f2, ny, 2, 1, KIND[kind], omega, magic, nsteps)
+    return f2, iold, inew
+
+
+def gpu_steps(f0, nx, ny, kind, omega, magic, nsteps, math_mode):
+    from plbm import LatticeGrid
+    g = LatticeGrid(nx, ny, collision=kind, math=math_mode)
+    g.set_relaxation(omega, magic)
+    g.upload(f0, 2)  # iold = 2 after alloc_grid
+    g.perform_lbm_step(nsteps)
+    return g
+
+
+@pytest.mark.parametrize("nx,ny", GRIDS)
+@pytest.mark.parametrize("kind,omega", [("bgk", 1.25), ("trt", 1.6), ("rr", 1.9)])
+def test_fused_step_strict_is_bit_identical(gpu_lib, nx, ny, kind, omega):
+    f0 = initial_state(nx, ny)
+    ref, iold, inew = oracle_steps(f0, ny, kind, omega, 0.25, 10)
+    g = gpu_steps(f0, nx, ny, kind, omega, 0.25, 10, "strict")
+    assert g.indices == (iold, inew)
+    got = g.download(g.iold)
+    assert np.array_equal(got[:, :, :ny], ref[iold - 1][:, :, :ny])
+    g.close()
+
+
+@pytest.mark.parametrize("nx,ny", GRIDS)
+@pytest.mark.parametrize("kind,omega", [("bgk", 1.25), ("trt", 1.6), ("rr", 1.9)])
+def test_fused_step_fma_within_1e12(gpu_lib, nx, ny, kind, omega):
+    f0 = initial_state(nx, ny)
+    ref, iold, _ = oracle_steps(f0, ny, kind, omega, 0.25, 50)
+    g = gpu_steps(f0, nx, ny, kind, omega, 0.25, 50, "fma")
+    got = g.download(g.iold)
+    r_ref = O.update_macros(ref[iold - 1], ny)
+    r_got = O.update_macros(got, ny)
+    for a, b in zip(r_got, r_ref):
+        assert relinf(a, b) <= TOL
+    assert relinf(got[:, :, :ny], ref[iold - 1][:, :, :ny]) <= TOL
+    g.close()
+
+
+@pytest.mark.parametrize("nx,ny", [(12, 32), (17, 13), (40, 16)])
+def test_bgk_improved(gpu_lib, nx, ny):
+    """collide_bgk_improved: fused when ld == ny, two passes on its (ny,nx) view otherwise."""
+    f0 = initial_state(nx, ny, u0=0.02)
+    ref, iold, _ = oracle_steps(f0, ny, "bgki", 1.3, 0.25, 3)
+    g = gpu_steps(f0, nx, ny, "bgki", 1.3, 0.25, 3, "strict")
+    got = g.download(g.iold)
+    if O.pad16(ny) == ny:
+        assert np.array_equal(got[:, :, :ny], ref[iold - 1][:, :, :ny])
+    else:
+        # the reference's sequence association touches the padded rows too
+        assert np.array_equal(got, ref[iold - 1])
+    g.close()
+
+
+@pytest.mark.parametrize("nx,ny", [(1, 1), (2, 3), (3, 2), (17, 13), (5, 40)])
+def test_stream_alone_is_bit_exact(gpu_lib, nx, ny):
+    """lbm_stream moves integers exactly: label every population by its index."""
+    from plbm import LatticeGrid
+    ld = O.pad16(ny)
+    src = np.arange(9 * nx * ld, dtype=np.float64).reshape(9, nx, ld)
+    g = LatticeGrid(nx, ny)
+    g.upload(src, g.iold)
+    g.stream()
+    got = g.download(g.inew)
+    ref = O.lbm_stream(src, ny)
+    assert np.array_equal(got[:, :, :ny], ref[:, :, :ny])
+    g.close()
+
+
+@pytest.mark.parametrize("kind", ["bgk", "trt", "rr"])
+def test_separate_stream_collide_equals_fused(gpu_lib, kind):
+    """grid%streaming() then grid%collision() then swap == perform_lbm_step."""
+    from plbm import LatticeGrid
+    nx, ny = 31, 21
+    f0 = initial_state(nx, ny)
+    a = LatticeGrid(nx, ny, collision=kind, math="strict")
+    b = LatticeGrid(nx, ny, collision=kind, math="strict")
+    for g in (a, b):
+        g.set_relaxation(1.7, 0.25)
+        g.upload(f0, 2)
+    for _ in range(4):
+        a.stream()
+        a.collide()
+        a.swap()
+    b.perform_lbm_step(4)
+    assert a.indices == b.indices
+    assert np.array_equal(a.download(a.iold)[:, :, :ny], b.download(b.iold)[:, :, :ny])
+    # and the collide kernel alone matches the oracle collision
+    f = f0.copy()
+    O.collide(f, ny, KIND[kind], 1.7, 0.25)
+    a.upload(f0, a.inew)
+    a.collide()
+    assert np.array_equal(a.download(a.inew)[:, :, :ny], f[:, :, :ny])
+    a.close()
+    b.close()
+
+
+def test_set_properties_and_equilibrium(gpu_lib):
+    from plbm import LatticeGrid
+    nx, ny = 23, 19
+    rng = np.random.default_rng(2)
+    rho = 1 + 1e-3 * rng.standard_normal((nx, ny))
+    ux, uy = 0.05 * rng.standard_normal((2, nx, ny))
+    g = LatticeGrid(nx, ny)
+    g.set_properties(0.1 / 3.0, 1.0)
+    tau, omega, magic = O.set_properties(0.1 / 3.0, 1.0)
+    pr = g.properties()
+    assert (pr["tau"], pr["omega"], pr["trt_magic"]) == (tau, omega, magic)
+    g.set_properties(0.02, 0.5, magic=0.25)
+    assert g.properties()["trt_magic"] == 0.25
+    g.set_pdf_to_equilibrium(rho, ux, uy)
+    got = g.download(g.iold)
+    ref = O.set_pdf_to_equilibrium(rho, ux, uy)
+    assert np.array_equal(got[:, :, :ny], ref[:, :, :ny])
+    g.close()
+
+
+def test_update_macros_reads_inew(gpu_lib):
+    """update_macros reads f(:,:,:,inew): after perform_lbm_step that is the
+    buffer streamed FROM in the last step (src/fvm_bardow.F90:351)."""
+    from plbm import LatticeGrid
+    nx, ny = 29, 17
+    f0 = initial_state(nx, ny)
+    g = gpu_steps(f0, nx, ny, "bgk", 1.4, 0.25, 7, "strict")
+    ref, iold, inew = oracle_steps(f0, ny, "bgk", 1.4, 0.25, 7)
+    rho, ux, uy = g.update_macros()
+    r = O.update_macros(ref[inew - 1], ny)
+    assert np.array_equal(rho, r[0]) and np.array_equal(ux, r[1]) and np.array_equal(uy, r[2])
+    g.close()
+
+
+@pytest.mark.parametrize("nx,ny", [(17, 13), (64, 48), (3, 5)])
+@pytest.mark.parametrize("order", [2, 4])
+def test_vorticity_bit_exact(gpu_lib, nx, ny, order):
+    from plbm import vorticity
+    rng = np.random.default_rng(order)
+    ux, uy = rng.standard_normal((2, nx, ny))
+    assert np.array_equal(vorticity(ux, uy, order), O.vorticity(ux, uy, order))
+
+
+def test_vorticity_standard_fourth_order(gpu_lib):
+    from plbm import vorticity
+    n = 64
+    x = (np.arange(n) + 0.5)[:, None] * 2 * np.pi / n
+    y = (np.arange(n) + 0.5)[None, :] * 2 * np.pi / n
+    ux = -np.cos(x) * np.sin(y) * np.ones((n, n))
+    uy = np.sin(x) * np.cos(y) * np.ones((n, n))
+    exact = 2 * np.cos(x) * np.cos(y) * (2 * np.pi / n)  # per-cell units
+    e2 = np.max(np.abs(vorticity(ux, uy, 2) - exact))
+    e44 = np.max(np.abs(vorticity(ux, uy, 44) - exact))
+    assert e44 < e2 / 50
+
+
+def test_reductions_binary64(gpu_lib):
+    from plbm import LatticeGrid
+    nx, ny = 120, 77
+    f0 = initial_state(nx, ny, u0=0.05)
+    g = LatticeGrid(nx, ny)
+    g.upload(f0, 1)
+    r, u, v = O.update_macros(f0, ny)
+    e_ref = O.kinetic_energy(r, u, v)
+    assert abs(g.kinetic_energy(1) - e_ref) <= 1e-13 * e_ref
+    uxa, uya = u * 1.01, v * 0.99
+    err = g.velocity_l2_error(uxa, uya, 1)
+    ref = math.sqrt(np.sum((u - uxa) ** 2 + (v - uya) ** 2) / np.sum(uxa ** 2 + uya ** 2))
+    assert abs(err - ref) <= 1e-12 * ref
+    g.close()
+
+
+def test_taylor_green_config_64(gpu_lib):
+    """TGV 64^2, BGK, rho0 = 1, u0 = 0.01, tau = 0.8, 1000 steps against the oracle and
+    the analytic decay exp(-2 nu k^2 t)."""
+    from plbm import LatticeGrid, cases
+    n, tau, u0 = 64, 0.8, 0.01
+    nu = (tau - 0.5) / 3.0
+    k = 2 * math.pi / n
+    p, ux, uy = cases.taylor_green(n, n, k, k, u0, nu)
+    rho = cases.tgv_density(p)
+    g = LatticeGrid(n, n, collision="bgk")
+    g.set_properties(nu, 1.0)
+    g.set_pdf_to_equilibrium(rho, ux, uy)
+    e0 = g.kinetic_energy(g.iold)
+    g.perform_lbm_step(1000)
+    f2 = np.stack([np.zeros((9, n, n)), O.set_pdf_to_equilibrium(rho, ux, uy)])
+    iold, _ = O.perform_lbm_step(f2, n, 2, 1, O.BGK, g.omega, 0.25, 1000)
+    got = g.download(g.iold)
+    for a, b in zip(O.update_macros(got, n), O.update_macros(f2[iold - 1], n)):
+        assert relinf(a, b) <= TOL
+    ratio = math.sqrt(g.kinetic_energy(g.iold) / e0)
+    assert abs(ratio / math.exp(-2 * nu * k * k * 1000) - 1) < 5e-3
+    g.close()
+
+
+def test_errors_are_reported(gpu_lib):
+    from plbm import LatticeGrid, PlbmError
+    g = LatticeGrid(8, 8)
+    with pytest.raises(PlbmError):
+        g.download(3)
+    with pytest.raises(PlbmError):
+        g.indices = (1, 1)
+    with pytest.raises(PlbmError):
+        g.collision = 9
+    d = LatticeGrid(8, 8, storage="f32dev")
+    with pytest.raises(PlbmError) as e:
+        d.collision = "bgki"
+    assert e.value.code == -4
+    g.close()
+    d.close()

@@ -1,0 +1,127 @@
+"""GPU tests of the plugin C ABI (sim/lbm.h semantics) against the oracle's
+restatement of sim/sim_slbm.F90 + sim/sim.F90, through SimPlugin."""
+import math
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def tgv_fields(nx, ny, umax=0.02, seed=0):
+    """TGV p, u (Fortran (nx,ny) order) as sim/cases.py:TGVStudy.solution builds them."""
+    rng = np.random.default_rng(seed)
+    x = (np.arange(nx) + 0.5)[:, None]
+    y = (np.arange(ny) + 0.5)[None, :]
+    kx, ky = 2 * math.pi / nx, 2 * math.pi / ny
+    u = np.empty((nx, ny, 2), order="F")
+    u[:, :, 0] = -umax * math.sqrt(ky / kx) * np.cos(kx * x) * np.sin(ky * y) + 1e-5 * rng.standard_normal((nx, ny))
+    u[:, :, 1] = umax * math.sqrt(kx / ky) * np.sin(kx * x) * np.cos(ky * y)
+    p = np.asfortranarray(-0.25 * umax ** 2 * ((ky / kx) * np.cos(2 * kx * x) + (kx / ky) * np.cos(2 * ky * y)))
+    return p, u
+
+
+def oracle_run(p, u, omega, nsteps):
+    # oracle plugin arrays are (ny, nx) C-order == (nx, ny) Fortran order
+    f = O.sim_eqinit(p.T, u[:, :, 0].T, u[:, :, 1].T)
+    f = O.sim_slbm_steps(f, omega, nsteps)
+    rho, ux, uy = O.sim_macros(f)
+    return rho.T, ux.T, uy.T
+
+
+@pytest.mark.parametrize("nx,ny", [(13, 11), (64, 64), (100, 37)])
+def test_plugin_strict_bit_identical(gpu_lib, nx, ny):
+    from plbm.plugin import SimPlugin, make_params
+    p, u = tgv_fields(nx, ny)
+    sim = SimPlugin()
+    sim.init((nx, ny), 1.0, p, u, params=make_params(math="strict"))
+    for _ in range(25):
+        sim.step(1.6)
+    rho, uu = sim.vars()
+    sim.free()
+    r, ux, uy = oracle_run(p, u, 1.6, 25)
+    assert np.array_equal(rho, r)
+    assert np.array_equal(uu[:, :, 0], ux) and np.array_equal(uu[:, :, 1], uy)
+
+
+def test_plugin_default_fma_within_1e12(gpu_lib):
+    from plbm.plugin import SimPlugin
+    nx, ny = 96, 80
+    p, u = tgv_fields(nx, ny)
+    sim = SimPlugin()
+    sim.init((nx, ny), 1.0, p, u)  # params = NULL, as sim/cases.py passes it
+    sim.steps(1.3, 200)
+    rho, uu = sim.vars()
+    sim.free()
+    r, ux, uy = oracle_run(p, u, 1.3, 200)
+    rel = lambda a, b: np.max(np.abs(a - b)) / np.max(np.abs(b))  # noqa: E731
+    assert rel(rho, r) <= 1e-12
+    assert rel(uu[:, :, 0], ux) <= 1e-12 and rel(uu[:, :, 1], uy) <= 1e-12
+
+
+def test_plugin_steps_equals_repeated_step(gpu_lib):
+    from plbm.plugin import SimPlugin
+    p, u = tgv_fields(20, 30)
+    a, b = SimPlugin(), SimPlugin()
+    a.init((20, 30), 1.0, p, u)
+    b.init((20, 30), 1.0, p, u)
+    for _ in range(9):
+        a.step(1.5)
+    b.steps(1.5, 9)
+    ra, ua = a.vars()
+    rb, ub = b.vars()
+    assert np.array_equal(ra, rb) and np.array_equal(ua, ub)
+    a.free()
+    b.free()
+
+
+def test_tgv_study_convergence_through_plugin(gpu_lib):
+    """The reference's TGV study (sim/cases.py:236-330) on this plugin: second-order
+    convergence of the L2 velocity error under grid refinement at fixed Re."""
+    from plbm.plugin import SimPlugin
+    cs = math.sqrt(1.0 / 3.0)
+    errs = []
+    for n in (16, 32, 64):
+        umax = 0.01 / (n / 16)
+        nu = umax * n / 10.0
+        tau = nu / cs ** 2
+        dt = 1.0
+        omega = dt / (tau + 0.5 * dt)
+        k = 2 * math.pi / n
+        td = 1.0 / (nu * 2 * k * k)
+        nsteps = round(-math.log(0.5) * td / dt)
+        x = (np.arange(n) + 0.5)[:, None]
+        y = (np.arange(n) + 0.5)[None, :]
+        u = np.empty((n, n, 2), order="F")
+        u[:, :, 0] = -umax * np.cos(k * x) * np.sin(k * y)
+        u[:, :, 1] = umax * np.sin(k * x) * np.cos(k * y)
+        p = np.asfortranarray(-0.25 * umax ** 2 * (np.cos(2 * k * x) + np.cos(2 * k * y)))
+        sim = SimPlugin()
+        sim.init((n, n), dt, p, u)
+        sim.steps(omega, nsteps)
+        _, uu = sim.vars()
+        sim.free()
+        decay = math.exp(-nsteps * dt / td)
+        ua = u * decay
+        mag = np.hypot(uu[:, :, 0], uu[:, :, 1])
+        mref = np.hypot(ua[:, :, 0], ua[:, :, 1])
+        errs.append(np.linalg.norm(mref - mag) / np.linalg.norm(mref))
+    assert errs[0] / errs[1] > 3.0 and errs[1] / errs[2] > 3.0, errs
+
+
+@pytest.mark.parametrize("kind", ["trt", "rr"])
+def test_plugin_other_collisions_conserve(gpu_lib, kind):
+    from plbm.plugin import SimPlugin, make_params
+    nx, ny = 40, 24
+    p, u = tgv_fields(nx, ny)
+    sim = SimPlugin()
+    sim.init((nx, ny), 1.0, p, u, params=make_params(kind=kind))
+    r0, u0 = sim.vars()
+    sim.steps(1.7, 50)
+    r1, u1 = sim.vars()
+    sim.free()
+    assert abs(r1.sum() - r0.sum()) < 1e-10 * r0.sum()
+    jx0, jx1 = (r0 * u0[:, :, 0]).sum(), (r1 * u1[:, :, 0]).sum()
+    assert abs(jx1 - jx0) < 1e-12
