@@ -9,7 +9,7 @@ perform_lbm_step (one fused pull-stream + collide kernel) over the grid.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                     [--n 8192] [--kind bgk|trt|rr] [--storage f64|f32dev|f16dev]
-                    [--math fma|strict|df64]
+                    [--math fma|strict|hybrid]
 
 Prints one JSON line (rank 0).  --impl reference times the reference's
 algorithm on the host cores instead: the C restatement of the Fortran
@@ -192,7 +192,7 @@ def main() -> None:
     ap.add_argument("--kind", default="bgk", choices=["bgk", "trt", "rr"])
     ap.add_argument("--tau", type=float, default=0.6)
     ap.add_argument("--storage", default="f64", choices=["f64", "f32dev", "f16dev"])
-    ap.add_argument("--math", default="fma", choices=["fma", "strict", "df64"])
+    ap.add_argument("--math", default="fma", choices=["fma", "strict", "hybrid"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU-baseline sample length")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
@@ -222,7 +222,9 @@ def main() -> None:
 
     n, omega = args.n, 1.0 / args.tau
     fields = initial_fields(n)
-    stream = torch.cuda.current_stream()
+    # a dedicated stream: the kernels and the timing events share it
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     g = LatticeGrid(n, n, storage=args.storage, collision=args.kind, math=args.math)
     g.set_stream(stream.cuda_stream)
     g.set_relaxation(omega, 0.25)
@@ -298,7 +300,7 @@ def main() -> None:
         "metric": "MLUPS", "value": mlups, "unit": "MLUPS", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": {"f64": "f64", "f32dev": "f32", "f16dev": "f16"}[args.storage] if args.math != "df64" else "f64 (df64 arithmetic)",
+        "dtype": {"f64": "f64", "f32dev": "f32", "f16dev": "f16"}[args.storage] ,
         "data": "synthetic (seeded TGV + noise, no dataset)",
         "config": workload_config(args),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

@@ -46,8 +46,9 @@ extern "C" {
 #define PLBM_MATH_FMA    0  /* binary64, FMA contraction allowed (default)   */
 #define PLBM_MATH_STRICT 1  /* binary64, no contraction: same operations and */
                             /* order as the Fortran, bit-identical to it     */
-#define PLBM_MATH_DF64   2  /* binary64 storage, arithmetic in unevaluated   */
-                            /* float pairs (hi+lo) on the FP32 pipe          */
+#define PLBM_MATH_HYBRID 2  /* BGK only: exact integer moments, double-float */
+                            /* nonlinear term, binary64 FMAs for the linear  */
+                            /* part; about 18 FP64 instructions per cell     */
 
 typedef struct plbm_grid plbm_grid_t;
 
@@ -130,6 +131,12 @@ int plbm_velocity_l2_error(plbm_grid_t *g, int ibuf, const double *uxa, const do
 
 /* Wait for all work queued on the handle's stream. */
 int plbm_synchronize(plbm_grid_t *g);
+
+/* PLBM_MATH_HYBRID needs |f_q| < 2 for every population; a kernel that met
+ * one outside sets a device flag.  Reads it (after synchronising the device)
+ * and clears it when reset != 0.  No reference counterpart (the reference has
+ * no such mode). */
+int plbm_hybrid_range_flag(int *flag, int reset);
 
 /* ---- raw device launches (device-resident callers: batched, autograd) ---- */
 /* One fused pull-stream + collide step over device lattices fsrc -> fdst

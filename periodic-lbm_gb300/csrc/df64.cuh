@@ -1,0 +1,246 @@
+// df64.cuh -- double-float ("df64") arithmetic: a value is the unevaluated
+// sum hi + lo of two binary32 numbers with |lo| <= ulp(hi)/2, about 48
+// significant bits.  All operations run on the FP32 pipe.
+//
+// Algorithms (error-free transformations):
+//   two_sum       Knuth, TAOCP vol. 2, 4.2.2 (6 flops)
+//   fast_two_sum  Dekker 1971, |a| >= |b| (3 flops)
+//   two_prod      with a fused multiply-add: p = a*b, e = fma(a, b, -p)
+//   add / mul     the "sloppy" double-length add and the FMA multiply of
+//                 Dekker 1971 / Hida-Li-Bailey QD library (2001), renormalised
+//                 by fast_two_sum.
+//   recip         one Newton step r1 = r0 + r0*(1 - b*r0) on a binary32
+//                 seed, evaluated in double-length arithmetic.
+// Conversions to and from binary64 use integer bit operations only: on GB300
+// F2F conversions between binary32 and binary64 run at the binary64 rate.
+//
+// Every function is __host__ __device__ so the same code can be checked on
+// the CPU.  Translation units using this header must be compiled without FMA
+// contraction (--fmad=false / -ffp-contract=off): the error-free
+// transformations assume each + - * is rounded separately, and the only
+// fused operations are the explicit fmaf calls.
+#pragma once
+#include <stdint.h>
+#include <string.h>
+#ifdef __CUDACC__
+#define DF_HD __host__ __device__ __forceinline__
+#else
+#include <math.h>
+#define DF_HD inline
+#endif
+
+namespace plbm {
+namespace df {
+
+struct df64 {
+  float hi, lo;
+};
+
+DF_HD float fmaf_(float a, float b, float c) {
+#ifdef __CUDA_ARCH__
+  return __fmaf_rn(a, b, c);
+#else
+  return fmaf(a, b, c);
+#endif
+}
+
+DF_HD uint32_t f2u(float f) {
+#ifdef __CUDA_ARCH__
+  return __float_as_uint(f);
+#else
+  uint32_t u;
+  memcpy(&u, &f, 4);
+  return u;
+#endif
+}
+DF_HD float u2f_bits(uint32_t u) {
+#ifdef __CUDA_ARCH__
+  return __uint_as_float(u);
+#else
+  float f;
+  memcpy(&f, &u, 4);
+  return f;
+#endif
+}
+DF_HD uint64_t d2u(double d) {
+#ifdef __CUDA_ARCH__
+  return (uint64_t)__double_as_longlong(d);
+#else
+  uint64_t u;
+  memcpy(&u, &d, 8);
+  return u;
+#endif
+}
+DF_HD double u2d(uint64_t u) {
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double((long long)u);
+#else
+  double d;
+  memcpy(&d, &u, 8);
+  return d;
+#endif
+}
+DF_HD float uint_to_float_rn(uint32_t u) {
+#ifdef __CUDA_ARCH__
+  return __uint2float_rn(u);
+#else
+  return (float)u;
+#endif
+}
+
+DF_HD df64 make(float hi, float lo) {
+  df64 r;
+  r.hi = hi;
+  r.lo = lo;
+  return r;
+}
+
+DF_HD df64 two_sum(float a, float b) {
+  float s = a + b;
+  float bb = s - a;
+  float e = (a - (s - bb)) + (b - bb);
+  return make(s, e);
+}
+
+DF_HD df64 fast_two_sum(float a, float b) {
+  float s = a + b;
+  float e = b - (s - a);
+  return make(s, e);
+}
+
+DF_HD df64 two_prod(float a, float b) {
+  float p = a * b;
+  float e = fmaf_(a, b, -p);
+  return make(p, e);
+}
+
+DF_HD df64 neg(df64 a) { return make(-a.hi, -a.lo); }
+
+DF_HD df64 add(df64 a, df64 b) {
+  df64 s = two_sum(a.hi, b.hi);
+  float e = s.lo + (a.lo + b.lo);
+  return fast_two_sum(s.hi, e);
+}
+
+DF_HD df64 sub(df64 a, df64 b) { return add(a, neg(b)); }
+
+DF_HD df64 add_f(df64 a, float b) {
+  df64 s = two_sum(a.hi, b);
+  float e = s.lo + a.lo;
+  return fast_two_sum(s.hi, e);
+}
+
+DF_HD df64 mul(df64 a, df64 b) {
+  df64 p = two_prod(a.hi, b.hi);
+  float e = fmaf_(a.hi, b.lo, p.lo);
+  e = fmaf_(a.lo, b.hi, e);
+  return fast_two_sum(p.hi, e);
+}
+
+DF_HD df64 mul_f(df64 a, float b) {
+  df64 p = two_prod(a.hi, b);
+  float e = fmaf_(a.lo, b, p.lo);
+  return fast_two_sum(p.hi, e);
+}
+
+DF_HD df64 sqr(df64 a) {
+  df64 p = two_prod(a.hi, a.hi);
+  float e = fmaf_(a.hi + a.hi, a.lo, p.lo);
+  return fast_two_sum(p.hi, e);
+}
+
+// Multiplication by a power of two is exact.
+DF_HD df64 mul_pow2(df64 a, float p2) { return make(a.hi * p2, a.lo * p2); }
+
+// 1/b: binary32 seed, one Newton step in double length.
+DF_HD df64 recip(df64 b) {
+  float r0 = 1.0f / b.hi;
+  // e = 1 - b*r0 in double length
+  df64 br = mul_f(b, r0);
+  df64 e = add_f(neg(br), 1.0f);
+  // r1 = r0 + r0*e
+  df64 re = mul_f(e, r0);
+  return add_f(re, r0);
+}
+
+// Split of a compile-time binary64 constant into hi + lo.
+DF_HD df64 from_double_const(double d) {
+  float hi = (float)d;
+  float lo = (float)(d - (double)hi);
+  return make(hi, lo);
+}
+
+// binary64 -> df64 by bit manipulation (no binary64 arithmetic, no F2F).
+// hi keeps the leading 24 significand bits (truncated), lo the next 29 bits
+// rounded to 24.  Magnitudes below 2^-126 become 0 (never reached by lattice
+// populations); NaN/Inf map to NaN/Inf in hi.
+DF_HD df64 from_double(double d) {
+  const uint64_t u = d2u(d);
+  const uint32_t H = (uint32_t)(u >> 32), L = (uint32_t)u;
+  const uint32_t sign = H & 0x80000000u;
+  const int e = (int)((H >> 20) & 0x7FFu);
+  const uint32_t mant23 = ((H & 0xFFFFFu) << 3) | (L >> 29);
+  if (e <= 896) return make(0.0f, 0.0f);
+  if (e >= 1151) return make(u2f_bits(sign | 0x7F800000u | (e == 2047 && ((H & 0xFFFFFu) | L) ? 0x400000u : 0u)), 0.0f);
+  const float hi = u2f_bits(sign | ((uint32_t)(e - 896) << 23) | mant23);
+  float lo = 0.0f;
+  if (e >= 949) {
+    // remainder r * 2^(e - 1075), r < 2^29
+    const float r = uint_to_float_rn(L & 0x1FFFFFFFu);
+    const float scale = u2f_bits((uint32_t)(e - 948) << 23);
+    lo = u2f_bits(f2u(r * scale) | sign);
+  }
+  return make(hi, lo);
+}
+
+// binary32 -> binary64 bit pattern (exact; binary32 subnormals become 0).
+DF_HD uint64_t float_bits_to_double_bits(float f) {
+  const uint32_t b = f2u(f);
+  const uint32_t ex = (b >> 23) & 0xFFu;
+  if (ex == 0) return (uint64_t)(b & 0x80000000u) << 32;
+  if (ex == 0xFF) return ((uint64_t)(b & 0x80000000u) << 32) | 0x7FF0000000000000ull |
+                         ((uint64_t)(b & 0x7FFFFFu) << 29);
+  const uint64_t hi = (uint64_t)((b & 0x80000000u) | ((ex + 896u) << 20) | ((b & 0x7FFFFFu) >> 3));
+  return (hi << 32) | (uint64_t)((b & 0x7u) << 29);
+}
+
+DF_HD double to_double_exactish(float f) { return u2d(float_bits_to_double_bits(f)); }
+
+// hi + lo rounded to binary64 without binary64 arithmetic.  For a
+// normalised pair (|lo| <= ulp(hi)/2) the 53-bit significand of hi + lo is
+// formed in a 64-bit integer: exact when lo reaches at most 29 bits below
+// hi's last bit, otherwise lo is rounded to the binary64 grid of hi
+// (half away from zero) before the add -- an error below 2^-53 |hi + lo|.
+DF_HD double pack_double(df64 a) {
+  const uint32_t bh = f2u(a.hi), bl = f2u(a.lo);
+  const uint32_t exh = (bh >> 23) & 0xFFu;
+  if (exh == 0 || exh == 0xFF) return to_double_exactish(a.hi);
+  const uint32_t exl = (bl >> 23) & 0xFFu;
+  // significand of hi on the binary64 grid: (2^23 + m) * 2^29
+  int64_t M = (int64_t)(0x800000u | (bh & 0x7FFFFFu)) << 29;
+  if (exl != 0) {
+    const int64_t ml = (int64_t)(0x800000u | (bl & 0x7FFFFFu));
+    // lo = ml * 2^(exl-150); grid unit of M is 2^(exh-127-52) => shift = exl - exh + 29
+    const int sh = (int)exl - (int)exh + 29;
+    int64_t li;
+    if (sh >= 0) li = ml << sh;
+    else if (sh > -25) li = (ml + ((int64_t)1 << (-sh - 1))) >> (-sh);
+    else li = 0;
+    if ((bl ^ bh) & 0x80000000u) M -= li;
+    else M += li;
+  }
+  int ex = (int)exh + 896;
+  if (M < ((int64_t)1 << 52)) {  // lo of opposite sign pulled below the binade
+    M <<= 1;
+    ex -= 1;
+  } else if (M >= ((int64_t)1 << 53)) {
+    M = (M + 1) >> 1;
+    ex += 1;
+  }
+  const uint64_t bits = ((uint64_t)(bh & 0x80000000u) << 32) | ((uint64_t)ex << 52) |
+                        ((uint64_t)M & 0xFFFFFFFFFFFFFull);
+  return u2d(bits);
+}
+
+}  // namespace df
+}  // namespace plbm

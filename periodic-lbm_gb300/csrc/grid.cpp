@@ -273,7 +273,7 @@ extern "C" int plbm_set_collision(plbm_grid_t* g, int kind) {
 
 extern "C" int plbm_set_math(plbm_grid_t* g, int math) {
   if (int r = check_grid(g)) return r;
-  if (math < PLBM_MATH_FMA || math > PLBM_MATH_DF64) return fail(PLBM_E_INVALID, "unknown math mode %d", math);
+  if (math < PLBM_MATH_FMA || math > PLBM_MATH_HYBRID) return fail(PLBM_E_INVALID, "unknown math mode %d", math);
   g->math = math;
   return PLBM_OK;
 }
@@ -355,7 +355,7 @@ cudaError_t fused_step(plbm_grid_t* g, const void* a, void* b, const CollParams&
   }
   switch (g->math) {
     case PLBM_MATH_STRICT: return strict::step_pull_f64(g->kind, s, p);
-    case PLBM_MATH_DF64: return step_pull_df64(g->kind, s, p);
+    case PLBM_MATH_HYBRID: return step_pull_df64(g->kind, s, p);
     default: return fma::step_pull_f64(g->kind, s, p);
   }
 }
@@ -387,8 +387,8 @@ extern "C" int plbm_collide(plbm_grid_t* g) {
 extern "C" int plbm_perform_lbm_step(plbm_grid_t* g, int nsteps) {
   if (int r = check_grid(g)) return r;
   if (nsteps < 0) return fail(PLBM_E_INVALID, "nsteps = %d < 0", nsteps);
-  if (g->math == PLBM_MATH_DF64 && g->storage == PLBM_F64 && g->kind == PLBM_BGKI)
-    return fail(PLBM_E_UNSUPPORTED, "PLBM_MATH_DF64 is not offered for collide_bgk_improved");
+  if (g->math == PLBM_MATH_HYBRID && g->storage == PLBM_F64 && g->kind != PLBM_BGK)
+    return fail(PLBM_E_UNSUPPORTED, "PLBM_MATH_HYBRID is offered for collide_bgk only");
   if (int r = use_device(g)) return r;
   const CollParams p = plbm_make_params(g->omega, g->trt_magic);
   for (int i = 0; i < nsteps; i++) {
@@ -515,6 +515,13 @@ extern "C" int plbm_synchronize(plbm_grid_t* g) {
   return ok();
 }
 
+extern "C" int plbm_hybrid_range_flag(int* flag, int reset) {
+  if (!flag) return fail(PLBM_E_INVALID, "flag is NULL");
+  CUDA_TRY(cudaDeviceSynchronize(), "synchronize");
+  CUDA_TRY(hybrid_range_flag(flag, reset), "read range flag");
+  return ok();
+}
+
 extern "C" int plbm_launch_step(int storage, int math, int kind, int nx, int ny, int ld, const void* fsrc,
                                 void* fdst, double omega, double trt_magic, void* stream) {
   if (nx < 1 || ny < 1 || ld < ny) return fail(PLBM_E_INVALID, "bad sizes nx=%d ny=%d ld=%d", nx, ny, ld);
@@ -526,8 +533,10 @@ extern "C" int plbm_launch_step(int storage, int math, int kind, int nx, int ny,
   if (storage == PLBM_F64) {
     if (kind == PLBM_BGKI && ld != ny)
       return fail(PLBM_E_UNSUPPORTED, "fused collide_bgk_improved needs ld == ny");
+    if (math == PLBM_MATH_HYBRID && kind != PLBM_BGK)
+      return fail(PLBM_E_UNSUPPORTED, "PLBM_MATH_HYBRID is offered for collide_bgk only");
     if (math == PLBM_MATH_STRICT) e = strict::step_pull_f64(kind, s, p);
-    else if (math == PLBM_MATH_DF64) e = step_pull_df64(kind, s, p);
+    else if (math == PLBM_MATH_HYBRID) e = step_pull_df64(kind, s, p);
     else e = fma::step_pull_f64(kind, s, p);
   } else if (storage == PLBM_F32DEV || storage == PLBM_F16DEV) {
     if (kind == PLBM_BGKI) return fail(PLBM_E_UNSUPPORTED, "collide_bgk_improved needs PLBM_F64 storage");

@@ -35,8 +35,9 @@ PLBM_DECLARE_F64(fma)
 PLBM_DECLARE_F64(strict)
 #undef PLBM_DECLARE_F64
 
-// binary64 storage, double-float arithmetic (YFast pull)
+// binary64 storage, hybrid arithmetic (hybrid.cuh), YFast pull, BGK only
 cudaError_t step_pull_df64(int kind, const Sweep& s, const CollParams& p);
+cudaError_t hybrid_range_flag(int* flag, int reset);
 
 // Deviation storage (storage = 1 float, 2 half), binary32 arithmetic.
 cudaError_t step_pull_dev(int storage, int kind, const Sweep& s, const CollParams& p);

@@ -8,9 +8,9 @@ binds it with ctypes and mirrors the reference's interfaces:
 * :mod:`plbm.plugin`  -- the sim/ plugin loader (``SimPlugin``);
 * :mod:`plbm.cases`   -- initial conditions of the benchmark cases.
 """
-from ._lib import (BGK, BGKI, F16DEV, F32DEV, F64, MATH_DF64, MATH_FMA, MATH_STRICT, RR, TRT,
+from ._lib import (BGK, BGKI, F16DEV, F32DEV, F64, MATH_HYBRID, MATH_FMA, MATH_STRICT, RR, TRT,
                    PlbmError, load)
 from .lattice import LatticeGrid, pad16, vorticity
 
 __all__ = ["LatticeGrid", "pad16", "vorticity", "load", "PlbmError", "BGK", "TRT", "RR", "BGKI",
-           "F64", "F32DEV", "F16DEV", "MATH_FMA", "MATH_STRICT", "MATH_DF64"]
+           "F64", "F32DEV", "F16DEV", "MATH_FMA", "MATH_STRICT", "MATH_HYBRID"]

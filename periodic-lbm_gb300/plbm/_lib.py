@@ -29,8 +29,8 @@ KINDS = {"bgk": BGK, "trt": TRT, "rr": RR, "bgki": BGKI}
 F64, F32DEV, F16DEV = 0, 1, 2
 STORAGES = {"f64": F64, "f32dev": F32DEV, "f16dev": F16DEV}
 # math
-MATH_FMA, MATH_STRICT, MATH_DF64 = 0, 1, 2
-MATHS = {"fma": MATH_FMA, "strict": MATH_STRICT, "df64": MATH_DF64}
+MATH_FMA, MATH_STRICT, MATH_HYBRID = 0, 1, 2
+MATHS = {"fma": MATH_FMA, "strict": MATH_STRICT, "hybrid": MATH_HYBRID}
 
 F16_SCALE_LOG2 = 15
 
@@ -85,6 +85,7 @@ SIGNATURES = {
     "plbm_kinetic_energy": (C.c_int, [_vp, C.c_int, _dp]),
     "plbm_velocity_l2_error": (C.c_int, [_vp, C.c_int, _vp, _vp, _dp]),
     "plbm_synchronize": (C.c_int, [_vp]),
+    "plbm_hybrid_range_flag": (C.c_int, [_ip, C.c_int]),
     "plbm_launch_step": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _vp, _vp,
                                    C.c_double, C.c_double, _vp]),
     # plugin ABI (include/plbm_plugin.h)

@@ -80,6 +80,36 @@ def test_fused_step_fma_within_1e12(gpu_lib, nx, ny, kind, omega):
     g.close()
 
 
+@pytest.mark.parametrize("nx,ny,steps,omega", [(17, 13, 10, 1.25), (64, 64, 1000, 1.6), (64, 64, 1000, 1.9),
+                                               (256, 192, 200, 1.25), (33, 48, 500, 1.8)])
+def test_hybrid_bgk_within_1e12(gpu_lib, nx, ny, steps, omega):
+    """PLBM_MATH_HYBRID (exact integer moments, double-float nonlinear term,
+    binary64 FMA relaxation) against the oracle at the binary64 tolerance."""
+    f0 = initial_state(nx, ny)
+    ref, iold, _ = oracle_steps(f0, ny, "bgk", omega, 0.25, steps)
+    g = gpu_steps(f0, nx, ny, "bgk", omega, 0.25, steps, "hybrid")
+    got = g.download(g.iold)
+    r_ref = O.update_macros(ref[iold - 1], ny)
+    r_got = O.update_macros(got, ny)
+    for a, b in zip(r_got, r_ref):
+        assert relinf(a, b) <= TOL
+    from plbm import _lib
+    import ctypes as C
+    flag = C.c_int(-1)
+    _lib.check(_lib.load().plbm_hybrid_range_flag(C.byref(flag), 1))
+    assert flag.value == 0
+    g.close()
+
+
+def test_hybrid_rejects_other_collisions(gpu_lib):
+    from plbm import LatticeGrid, PlbmError
+    g = LatticeGrid(16, 16, collision="trt", math="hybrid")
+    with pytest.raises(PlbmError) as e:
+        g.perform_lbm_step(1)
+    assert e.value.code == -4
+    g.close()
+
+
 @pytest.mark.parametrize("nx,ny", [(12, 32), (17, 13), (40, 16)])
 def test_bgk_improved(gpu_lib, nx, ny):
     """collide_bgk_improved: fused when ld == ny, two passes on its (ny,nx) view otherwise."""
