@@ -30,6 +30,7 @@ UNITS = [
     ("step_dev.cu", "step_dev.o", ["--fmad=true"]),
     ("step_df64.cu", "step_df64.o", ["--fmad=false"]),
     ("fields.cu", "fields.o", ["--fmad=false"]),
+    ("noalloc.cu", "noalloc.o", ["--fmad=false"]),
     ("batched.cu", "batched.o", ["--fmad=true"]),
     ("adjoint.cu", "adjoint.o", ["--fmad=true"]),
     ("grid.cpp", "grid.o", ["-x", "cu", "--fmad=false"]),

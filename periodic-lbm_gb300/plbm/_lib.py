@@ -86,6 +86,7 @@ SIGNATURES = {
     "plbm_velocity_l2_error": (C.c_int, [_vp, C.c_int, _vp, _vp, _dp]),
     "plbm_synchronize": (C.c_int, [_vp]),
     "plbm_hybrid_range_flag": (C.c_int, [_ip, C.c_int]),
+    "plbm_velocity_l2_error_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _dp, _vp]),
     "plbm_launch_step": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _vp, _vp,
                                    C.c_double, C.c_double, _vp]),
     # plugin ABI (include/plbm_plugin.h)
