@@ -159,6 +159,59 @@ int plbm_synchronize(plbm_grid_t *g);
  * no such mode). */
 int plbm_hybrid_range_flag(int *flag, int reset);
 
+/* ---- batched grids ------------------------------------------------------
+ * Many independent periodic grids of uneven sizes and relaxation times,
+ * stepped together.  No counterpart in the reference (it steps one
+ * lattice_grid at a time); each grid's step is the reference's
+ * perform_lbm_step with collide_bgk or collide_trt (incompressible TRT with
+ * the grid's magic parameter).  Every grid keeps the layout f(ld,nx,0:8),
+ * ld = pad16(ny), with two lattices packed in one allocation.
+ *
+ * Work is cut into tiles of ty rows (y) x threads/ty columns of one grid;
+ * ty is chosen per grid from the bucket of its ny (<=48, <=96, <=192,
+ * <=384, >384).  persistent = 1 runs all steps of a plbm_batch_run in ONE
+ * cooperative launch with a grid-wide barrier between steps (bounded wait:
+ * an expired wait is reported as PLBM_E_TIMEOUT by plbm_batch_synchronize);
+ * persistent = 0 launches once per step.  Either can be captured into a CUDA
+ * graph with plbm_batch_capture and replayed with plbm_batch_launch_graph. */
+#define PLBM_BATCH_BUCKETS 5
+typedef struct plbm_batch_schedule {
+    int threads;       /* threads per CTA, multiple of 32 in [64, 512]          */
+    int ctas_per_sm;   /* resident CTAs per SM, 0 = occupancy maximum           */
+    int persistent;    /* 1 = one cooperative launch for all steps              */
+    int ty[PLBM_BATCH_BUCKETS]; /* tile rows per ny bucket, power of 2 >= 32    */
+} plbm_batch_schedule;
+typedef struct plbm_batch plbm_batch_t;
+
+int plbm_batch_default_schedule(plbm_batch_schedule *s);
+/* kind[i] in {PLBM_BGK, PLBM_TRT}; trt_magic may be NULL (0.25);
+ * storage PLBM_F64 or PLBM_F32DEV.  All lattices start at 0. */
+int plbm_batch_create(int ngrids, const int *nx, const int *ny, const int *kind,
+                      const double *omega, const double *trt_magic, int storage,
+                      plbm_batch_t **out);
+int plbm_batch_destroy(plbm_batch_t *b);
+int plbm_batch_info(const plbm_batch_t *b, int *ngrids, long long *cells, int *ntiles, int *ctas);
+int plbm_batch_set_schedule(plbm_batch_t *b, const plbm_batch_schedule *s);
+int plbm_batch_get_schedule(const plbm_batch_t *b, plbm_batch_schedule *s);
+int plbm_batch_set_stream(plbm_batch_t *b, void *cuda_stream);
+/* Equilibrium of host (ny,nx) rho/ux/uy into the current lattice of grid i
+ * (set_pdf_to_equilibrium, src/fvm_bardow.F90:272-305). */
+int plbm_batch_set_equilibrium(plbm_batch_t *b, int grid, const double *rho, const double *ux,
+                               const double *uy);
+/* Queue nsteps steps of every grid (asynchronous). */
+int plbm_batch_run(plbm_batch_t *b, int nsteps);
+/* Capture nsteps steps into a CUDA graph for the current step parity. */
+int plbm_batch_capture(plbm_batch_t *b, int nsteps);
+int plbm_batch_launch_graph(plbm_batch_t *b);
+/* Wait; PLBM_E_TIMEOUT if a persistent run's barrier wait expired. */
+int plbm_batch_synchronize(plbm_batch_t *b);
+int plbm_batch_steps(const plbm_batch_t *b, long long *steps);
+/* Moments (update_macros order for PLBM_F64) of grid i's current state into
+ * host (ny,nx) arrays; any may be NULL.  Synchronises. */
+int plbm_batch_macros(plbm_batch_t *b, int grid, double *rho, double *ux, double *uy);
+/* Current lattice of grid i as binary64 f(ld,nx,0:8) on the host. */
+int plbm_batch_download(plbm_batch_t *b, int grid, double *f);
+
 /* ---- raw device launches (device-resident callers: batched, autograd) ---- */
 /* One fused pull-stream + collide step over device lattices fsrc -> fdst
  * (layout above, PLBM_F64 storage = double, F32DEV = float, F16DEV = half). */

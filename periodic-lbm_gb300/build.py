@@ -35,6 +35,7 @@ UNITS = [
     ("adjoint.cu", "adjoint.o", ["--fmad=true"]),
     ("grid.cpp", "grid.o", ["-x", "cu", "--fmad=false"]),
     ("plugin.cpp", "plugin.o", ["-x", "cu", "--fmad=false"]),
+    ("batch.cpp", "batch.o", ["-x", "cu", "--fmad=false"]),
 ]
 
 

@@ -1,0 +1,386 @@
+// batch.cpp -- plbm_batch_* C ABI: many periodic grids of uneven sizes and
+// relaxation times stepped together (see batched.cu for the kernels).
+#include <cuda_runtime.h>
+#include <string.h>
+#include <algorithm>
+#include <vector>
+
+#include "../../include/plbm_gpu.h"
+#include "plbm_batched.h"
+#include "plbm_launch.h"
+
+namespace plbm_internal {
+int fail(int code, const char* fmt, ...);
+int cuda_fail(cudaError_t e, const char* what);
+}  // namespace plbm_internal
+using plbm_internal::cuda_fail;
+using plbm_internal::fail;
+using namespace plbm;
+CollParams plbm_make_params(double omega, double trt_magic);
+
+#define CUDA_TRY(expr, what)                            \
+  do {                                                  \
+    cudaError_t e_ = (expr);                            \
+    if (e_ != cudaSuccess) return cuda_fail(e_, what);  \
+  } while (0)
+
+struct plbm_batch {
+  int ngrids = 0, storage = 0, device = 0, sms = 0;
+  std::vector<BatchGrid> grids;   // host copy (off, sizes, params, ty)
+  BatchGrid* d_grids = nullptr;
+  int* d_tile_start = nullptr;
+  int ntiles = 0;
+  long long cells = 0;
+  size_t elems = 0, elem_bytes = 8;
+  void* base = nullptr;
+  void* ctrl = nullptr;
+  double* scratch = nullptr;
+  size_t scratch_elems = 0;
+  cudaStream_t own = nullptr, stream = nullptr;
+  plbm_batch_schedule sched{};
+  int ctas = 0;
+  long long steps_done = 0;
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  int graph_steps[2] = {0, 0};
+};
+
+namespace {
+
+int pad16(int n) { return n % 16 ? n + (16 - n % 16) : n; }
+
+int bucket_of(int ny) {
+  return ny <= 48 ? 0 : ny <= 96 ? 1 : ny <= 192 ? 2 : ny <= 384 ? 3 : 4;
+}
+
+int check_schedule(const plbm_batch_schedule& s) {
+  if (s.threads < 64 || s.threads > kBatchMaxThreads || (s.threads & 31))
+    return fail(PLBM_E_INVALID, "schedule.threads = %d: need a multiple of 32 in [64, %d]", s.threads,
+                kBatchMaxThreads);
+  if (s.ctas_per_sm < 0 || s.ctas_per_sm > 32) return fail(PLBM_E_INVALID, "schedule.ctas_per_sm = %d", s.ctas_per_sm);
+  for (int i = 0; i < PLBM_BATCH_BUCKETS; i++) {
+    const int ty = s.ty[i];
+    if (ty < 32 || ty > s.threads || (ty & (ty - 1)) || s.threads % ty)
+      return fail(PLBM_E_INVALID, "schedule.ty[%d] = %d: need a power of two >= 32 dividing threads=%d", i, ty,
+                  s.threads);
+  }
+  return PLBM_OK;
+}
+
+void drop_graphs(plbm_batch_t* b) {
+  for (int i = 0; i < 2; i++) {
+    if (b->graph[i]) cudaGraphExecDestroy(b->graph[i]);
+    b->graph[i] = nullptr;
+    b->graph_steps[i] = 0;
+  }
+}
+
+int apply_schedule(plbm_batch_t* b) {
+  std::vector<int> start(b->ngrids + 1, 0);
+  for (int i = 0; i < b->ngrids; i++) {
+    BatchGrid& g = b->grids[i];
+    g.ty = b->sched.ty[bucket_of(g.ny)];
+    const int tx = b->sched.threads / g.ty;
+    const long long t = (long long)((g.ny + g.ty - 1) / g.ty) * ((g.nx + tx - 1) / tx);
+    if ((long long)start[i] + t > 0x7fffffffLL) return fail(PLBM_E_INVALID, "too many tiles");
+    start[i + 1] = start[i] + (int)t;
+  }
+  b->ntiles = start[b->ngrids];
+  CUDA_TRY(cudaMemcpy(b->d_grids, b->grids.data(), sizeof(BatchGrid) * b->ngrids, cudaMemcpyHostToDevice),
+           "upload batch table");
+  CUDA_TRY(cudaMemcpy(b->d_tile_start, start.data(), sizeof(int) * (b->ngrids + 1), cudaMemcpyHostToDevice),
+           "upload tile table");
+  int per_sm = 0;
+  CUDA_TRY(batch_max_ctas(b->storage, b->sched.threads, &per_sm), "occupancy");
+  if (per_sm < 1) return fail(PLBM_E_UNSUPPORTED, "batched kernel does not fit on an SM with %d threads", b->sched.threads);
+  const int want = b->sched.ctas_per_sm > 0 ? std::min(b->sched.ctas_per_sm, per_sm) : per_sm;
+  b->ctas = std::max(1, std::min(b->ntiles, want * b->sms));
+  drop_graphs(b);
+  return PLBM_OK;
+}
+
+BatchLaunch launch_of(const plbm_batch_t* b) {
+  BatchLaunch L;
+  L.grids = b->d_grids;
+  L.tile_start = b->d_tile_start;
+  L.ngrids = b->ngrids;
+  L.ntiles = b->ntiles;
+  L.threads = b->sched.threads;
+  L.ctas = b->ctas;
+  L.persistent = b->sched.persistent;
+  L.base = b->base;
+  L.ctrl = b->ctrl;
+  L.stream = b->stream;
+  return L;
+}
+
+// Queue nsteps (control-block reset + launches) on the batch stream.
+cudaError_t enqueue(plbm_batch_t* b, int nsteps) {
+  if (b->sched.persistent) {
+    cudaError_t e = cudaMemsetAsync(b->ctrl, 0, batch_ctrl_bytes(), b->stream);
+    if (e != cudaSuccess) return e;
+  }
+  return batch_run(b->storage, launch_of(b), nsteps, (int)(b->steps_done & 1));
+}
+
+void* lattice_of(const plbm_batch_t* b, int gi, int which) {
+  const BatchGrid& g = b->grids[gi];
+  const size_t lat = (size_t)g.ld * g.nx * 9;
+  return static_cast<char*>(b->base) + ((size_t)g.off + (which ? lat : 0)) * b->elem_bytes;
+}
+
+int current(const plbm_batch_t* b) { return (int)(b->steps_done & 1); }
+
+int ensure_scratch(plbm_batch_t* b, size_t n) {
+  if (b->scratch_elems >= n) return PLBM_OK;
+  if (b->scratch) cudaFree(b->scratch);
+  b->scratch = nullptr;
+  b->scratch_elems = 0;
+  CUDA_TRY(cudaMalloc(&b->scratch, n * sizeof(double)), "cudaMalloc(batch scratch)");
+  b->scratch_elems = n;
+  return PLBM_OK;
+}
+
+}  // namespace
+
+extern "C" int plbm_batch_default_schedule(plbm_batch_schedule* s) {
+  if (!s) return fail(PLBM_E_INVALID, "NULL schedule");
+  s->threads = 256;
+  s->ctas_per_sm = 0;
+  s->persistent = 1;
+  const int ty[PLBM_BATCH_BUCKETS] = {32, 64, 128, 256, 256};
+  for (int i = 0; i < PLBM_BATCH_BUCKETS; i++) s->ty[i] = ty[i];
+  return PLBM_OK;
+}
+
+extern "C" int plbm_batch_create(int ngrids, const int* nx, const int* ny, const int* kind, const double* omega,
+                                 const double* trt_magic, int storage, plbm_batch_t** out) {
+  if (!out) return fail(PLBM_E_INVALID, "out is NULL");
+  *out = nullptr;
+  if (ngrids < 1 || !nx || !ny || !kind || !omega) return fail(PLBM_E_INVALID, "bad batch description");
+  if (storage != PLBM_F64 && storage != PLBM_F32DEV)
+    return fail(PLBM_E_UNSUPPORTED, "batched storage %d (PLBM_F64 or PLBM_F32DEV)", storage);
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+    cudaGetLastError();
+    return fail(PLBM_E_NODEVICE, "no CUDA device visible");
+  }
+  plbm_batch_t* b = new plbm_batch_t();
+  b->ngrids = ngrids;
+  b->storage = storage;
+  b->elem_bytes = storage == PLBM_F64 ? 8 : 4;
+  cudaGetDevice(&b->device);
+  cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, b->device);
+  b->grids.resize(ngrids);
+  size_t off = 0;
+  for (int i = 0; i < ngrids; i++) {
+    if (nx[i] < 1 || ny[i] < 1 || (kind[i] != PLBM_BGK && kind[i] != PLBM_TRT) || !(omega[i] > 0 && omega[i] < 2)) {
+      delete b;
+      return fail(PLBM_E_INVALID, "grid %d: nx=%d ny=%d kind=%d omega=%g (BGK or TRT, 0<omega<2)", i, nx[i], ny[i],
+                  kind[i], omega[i]);
+    }
+    BatchGrid& g = b->grids[i];
+    memset(&g, 0, sizeof g);
+    g.nx = nx[i];
+    g.ny = ny[i];
+    g.ld = pad16(ny[i]);
+    g.kind = kind[i];
+    g.p = plbm_make_params(omega[i], trt_magic ? trt_magic[i] : 0.25);
+    g.off = (long long)off;
+    off += 2 * (size_t)g.ld * g.nx * 9;
+    b->cells += (long long)g.nx * g.ny;
+  }
+  b->elems = off;
+  cudaError_t e = cudaMalloc(&b->base, off * b->elem_bytes);
+  if (e == cudaSuccess) e = cudaMemset(b->base, 0, off * b->elem_bytes);
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_grids, sizeof(BatchGrid) * ngrids);
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_tile_start, sizeof(int) * (ngrids + 1));
+  if (e == cudaSuccess) e = cudaMalloc(&b->ctrl, batch_ctrl_bytes());
+  if (e == cudaSuccess) e = cudaMemset(b->ctrl, 0, batch_ctrl_bytes());
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->own, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    plbm_batch_destroy(b);
+    return cuda_fail(e, "batch allocation");
+  }
+  b->stream = b->own;
+  plbm_batch_default_schedule(&b->sched);
+  if (int r = apply_schedule(b)) {
+    plbm_batch_destroy(b);
+    return r;
+  }
+  *out = b;
+  return PLBM_OK;
+}
+
+extern "C" int plbm_batch_destroy(plbm_batch_t* b) {
+  if (!b) return PLBM_OK;
+  cudaSetDevice(b->device);
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  drop_graphs(b);
+  cudaFree(b->base);
+  cudaFree(b->d_grids);
+  cudaFree(b->d_tile_start);
+  cudaFree(b->ctrl);
+  cudaFree(b->scratch);
+  if (b->own) cudaStreamDestroy(b->own);
+  delete b;
+  return PLBM_OK;
+}
+
+extern "C" int plbm_batch_info(const plbm_batch_t* b, int* ngrids, long long* cells, int* ntiles, int* ctas) {
+  if (!b) return fail(PLBM_E_INVALID, "NULL batch");
+  if (ngrids) *ngrids = b->ngrids;
+  if (cells) *cells = b->cells;
+  if (ntiles) *ntiles = b->ntiles;
+  if (ctas) *ctas = b->ctas;
+  return PLBM_OK;
+}
+
+extern "C" int plbm_batch_set_schedule(plbm_batch_t* b, const plbm_batch_schedule* s) {
+  if (!b || !s) return fail(PLBM_E_INVALID, "NULL argument");
+  if (int r = check_schedule(*s)) return r;
+  CUDA_TRY(cudaSetDevice(b->device), "cudaSetDevice");
+  CUDA_TRY(cudaStreamSynchronize(b->stream), "synchronize");
+  b->sched = *s;
+  return apply_schedule(b);
+}
+
+extern "C" int plbm_batch_get_schedule(const plbm_batch_t* b, plbm_batch_schedule* s) {
+  if (!b || !s) return fail(PLBM_E_INVALID, "NULL argument");
+  *s = b->sched;
+  return PLBM_OK;
+}
+
+extern "C" int plbm_batch_set_stream(plbm_batch_t* b, void* stream) {
+  if (!b) return fail(PLBM_E_INVALID, "NULL batch");
+  b->stream = stream ? static_cast<cudaStream_t>(stream) : b->own;
+  drop_graphs(b);
+  return PLBM_OK;
+}
+
+extern "C" int plbm_batch_set_equilibrium(plbm_batch_t* b, int grid, const double* rho, const double* ux,
+                                          const double* uy) {
+  if (!b) return fail(PLBM_E_INVALID, "NULL batch");
+  if (grid < 0 || grid >= b->ngrids) return fail(PLBM_E_INVALID, "grid index %d outside 0..%d", grid, b->ngrids - 1);
+  if (!rho || !ux || !uy) return fail(PLBM_E_INVALID, "NULL field");
+  CUDA_TRY(cudaSetDevice(b->device), "cudaSetDevice");
+  const BatchGrid& g = b->grids[grid];
+  const size_t n = (size_t)g.nx * g.ny;
+  if (int r = ensure_scratch(b, 3 * n)) return r;
+  double* d = b->scratch;
+  CUDA_TRY(cudaMemcpyAsync(d, rho, n * 8, cudaMemcpyHostToDevice, b->stream), "upload rho");
+  CUDA_TRY(cudaMemcpyAsync(d + n, ux, n * 8, cudaMemcpyHostToDevice, b->stream), "upload ux");
+  CUDA_TRY(cudaMemcpyAsync(d + 2 * n, uy, n * 8, cudaMemcpyHostToDevice, b->stream), "upload uy");
+  const int st = b->storage == PLBM_F64 ? ST_F64 : ST_F32DEV;
+  CUDA_TRY(equilibrium(st, 0, g.nx, g.ny, g.ld, d, d + n, d + 2 * n, 0, lattice_of(b, grid, current(b)), b->stream),
+           "equilibrium kernel");
+  CUDA_TRY(cudaStreamSynchronize(b->stream), "equilibrium sync");
+  return PLBM_OK;
+}
+
+extern "C" int plbm_batch_run(plbm_batch_t* b, int nsteps) {
+  if (!b) return fail(PLBM_E_INVALID, "NULL batch");
+  if (nsteps < 0) return fail(PLBM_E_INVALID, "nsteps = %d < 0", nsteps);
+  CUDA_TRY(cudaSetDevice(b->device), "cudaSetDevice");
+  CUDA_TRY(enqueue(b, nsteps), "batched step launch");
+  b->steps_done += nsteps;
+  return PLBM_OK;
+}
+
+extern "C" int plbm_batch_capture(plbm_batch_t* b, int nsteps) {
+  if (!b) return fail(PLBM_E_INVALID, "NULL batch");
+  if (nsteps < 1) return fail(PLBM_E_INVALID, "nsteps = %d < 1", nsteps);
+  CUDA_TRY(cudaSetDevice(b->device), "cudaSetDevice");
+  const int par = current(b);
+  if (b->graph[par]) {
+    cudaGraphExecDestroy(b->graph[par]);
+    b->graph[par] = nullptr;
+  }
+  cudaStream_t cap = nullptr;
+  CUDA_TRY(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking), "capture stream");
+  cudaStream_t keep = b->stream;
+  b->stream = cap;
+  cudaGraph_t graph = nullptr;
+  cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    cudaError_t el = enqueue(b, nsteps);
+    e = cudaStreamEndCapture(cap, &graph);
+    if (el != cudaSuccess) e = el;
+  }
+  b->stream = keep;
+  cudaStreamDestroy(cap);
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&b->graph[par], graph, 0);
+  if (graph) cudaGraphDestroy(graph);
+  if (e != cudaSuccess) {
+    b->graph[par] = nullptr;
+    return cuda_fail(e, "graph capture of the batched step");
+  }
+  b->graph_steps[par] = nsteps;
+  return PLBM_OK;
+}
+
+extern "C" int plbm_batch_launch_graph(plbm_batch_t* b) {
+  if (!b) return fail(PLBM_E_INVALID, "NULL batch");
+  const int par = current(b);
+  if (!b->graph[par])
+    return fail(PLBM_E_INVALID, "no graph captured for the current step parity (call plbm_batch_capture)");
+  CUDA_TRY(cudaSetDevice(b->device), "cudaSetDevice");
+  CUDA_TRY(cudaGraphLaunch(b->graph[par], b->stream), "cudaGraphLaunch");
+  b->steps_done += b->graph_steps[par];
+  return PLBM_OK;
+}
+
+extern "C" int plbm_batch_synchronize(plbm_batch_t* b) {
+  if (!b) return fail(PLBM_E_INVALID, "NULL batch");
+  CUDA_TRY(cudaSetDevice(b->device), "cudaSetDevice");
+  CUDA_TRY(cudaStreamSynchronize(b->stream), "synchronize");
+  if (b->sched.persistent) {
+    int err = 0, where = 0;
+    CUDA_TRY(batch_read_ctrl(b->ctrl, &err, &where, b->stream), "read control block");
+    if (err) return fail(PLBM_E_TIMEOUT, "batched persistent kernel: grid barrier wait expired at step %d", where);
+  }
+  return PLBM_OK;
+}
+
+extern "C" int plbm_batch_steps(const plbm_batch_t* b, long long* steps) {
+  if (!b || !steps) return fail(PLBM_E_INVALID, "NULL argument");
+  *steps = b->steps_done;
+  return PLBM_OK;
+}
+
+extern "C" int plbm_batch_macros(plbm_batch_t* b, int grid, double* rho, double* ux, double* uy) {
+  if (!b) return fail(PLBM_E_INVALID, "NULL batch");
+  if (grid < 0 || grid >= b->ngrids) return fail(PLBM_E_INVALID, "grid index %d outside 0..%d", grid, b->ngrids - 1);
+  if (int r = plbm_batch_synchronize(b)) return r;
+  const BatchGrid& g = b->grids[grid];
+  const size_t n = (size_t)g.nx * g.ny;
+  if (int r = ensure_scratch(b, 3 * n)) return r;
+  double* d = b->scratch;
+  const int st = b->storage == PLBM_F64 ? ST_F64 : ST_F32DEV;
+  CUDA_TRY(macros(st, 0, g.nx, g.ny, g.ld, lattice_of(b, grid, current(b)), d, d + n, d + 2 * n, b->stream),
+           "moments kernel");
+  if (rho) CUDA_TRY(cudaMemcpyAsync(rho, d, n * 8, cudaMemcpyDeviceToHost, b->stream), "download rho");
+  if (ux) CUDA_TRY(cudaMemcpyAsync(ux, d + n, n * 8, cudaMemcpyDeviceToHost, b->stream), "download ux");
+  if (uy) CUDA_TRY(cudaMemcpyAsync(uy, d + 2 * n, n * 8, cudaMemcpyDeviceToHost, b->stream), "download uy");
+  CUDA_TRY(cudaStreamSynchronize(b->stream), "macros sync");
+  return PLBM_OK;
+}
+
+extern "C" int plbm_batch_download(plbm_batch_t* b, int grid, double* f) {
+  if (!b || !f) return fail(PLBM_E_INVALID, "NULL argument");
+  if (grid < 0 || grid >= b->ngrids) return fail(PLBM_E_INVALID, "grid index %d outside 0..%d", grid, b->ngrids - 1);
+  if (int r = plbm_batch_synchronize(b)) return r;
+  const BatchGrid& g = b->grids[grid];
+  const size_t lat = (size_t)g.ld * g.nx * 9;
+  if (b->storage == PLBM_F64) {
+    CUDA_TRY(cudaMemcpyAsync(f, lattice_of(b, grid, current(b)), lat * 8, cudaMemcpyDeviceToHost, b->stream),
+             "download lattice");
+  } else {
+    if (int r = ensure_scratch(b, lat)) return r;
+    CUDA_TRY(cudaMemsetAsync(b->scratch, 0, lat * 8, b->stream), "clear staging");
+    CUDA_TRY(dev_to_f64(ST_F32DEV, g.nx, g.ny, g.ld, lattice_of(b, grid, current(b)), b->scratch, b->stream),
+             "convert lattice");
+    CUDA_TRY(cudaMemcpyAsync(f, b->scratch, lat * 8, cudaMemcpyDeviceToHost, b->stream), "download lattice");
+  }
+  CUDA_TRY(cudaStreamSynchronize(b->stream), "download sync");
+  return PLBM_OK;
+}

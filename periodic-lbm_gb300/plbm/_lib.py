@@ -89,6 +89,22 @@ SIGNATURES = {
     "plbm_velocity_l2_error_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _dp, _vp]),
     "plbm_launch_step": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _vp, _vp,
                                    C.c_double, C.c_double, _vp]),
+    # batched grids
+    "plbm_batch_default_schedule": (C.c_int, [_vp]),
+    "plbm_batch_create": (C.c_int, [C.c_int, _vp, _vp, _vp, _vp, _vp, C.c_int, C.POINTER(_vp)]),
+    "plbm_batch_destroy": (C.c_int, [_vp]),
+    "plbm_batch_info": (C.c_int, [_vp, _ip, C.POINTER(C.c_longlong), _ip, _ip]),
+    "plbm_batch_set_schedule": (C.c_int, [_vp, _vp]),
+    "plbm_batch_get_schedule": (C.c_int, [_vp, _vp]),
+    "plbm_batch_set_stream": (C.c_int, [_vp, _vp]),
+    "plbm_batch_set_equilibrium": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp]),
+    "plbm_batch_run": (C.c_int, [_vp, C.c_int]),
+    "plbm_batch_capture": (C.c_int, [_vp, C.c_int]),
+    "plbm_batch_launch_graph": (C.c_int, [_vp]),
+    "plbm_batch_synchronize": (C.c_int, [_vp]),
+    "plbm_batch_steps": (C.c_int, [_vp, C.POINTER(C.c_longlong)]),
+    "plbm_batch_macros": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp]),
+    "plbm_batch_download": (C.c_int, [_vp, C.c_int, _vp]),
     # plugin ABI (include/plbm_plugin.h)
     "c_plbmgpu_init": (_vp, [C.c_int, C.c_int, C.c_double, _vp, _vp, _vp, _vp]),
     "c_plbmgpu_step": (None, [_vp, C.c_double]),

@@ -121,6 +121,26 @@ def test_cases_match_oracle_initial_conditions():
         assert np.max(np.abs(a - b)) <= 1e-15 * max(1.0, np.max(np.abs(b)))
 
 
+def test_batch_default_schedule_and_workload(lib):
+    from plbm import batched
+    s = batched.default_schedule()
+    assert s.threads == 256 and s.persistent == 1 and list(s.ty) == [32, 64, 128, 256, 256]
+    specs, fields = batched.random_tgv_batch(512, seed=2024)
+    cells = sum(sp.nx * sp.ny for sp in specs)
+    assert 25e6 < cells < 70e6  # expected ~42 M for log-uniform sizes in [32, 1024]
+    assert all(32 <= sp.nx <= 1024 and 32 <= sp.ny <= 1024 for sp in specs)
+    assert all(0.51 <= 1 / sp.omega <= 1.5 for sp in specs)
+    kinds = [sp.kind for sp in specs]
+    assert 0.4 < kinds.count("bgk") / len(kinds) < 0.6
+    assert all(1 <= f[2] <= 4 and 1 <= f[3] <= 4 and 0.005 <= f[4] <= 0.05 for f in fields)
+
+
+def test_batch_bucket_edges_match_library():
+    from plbm import autotune
+    assert [autotune.bucket_of(n) for n in (1, 48, 49, 96, 97, 192, 193, 384, 385, 5000)] == \
+        [0, 0, 1, 1, 2, 2, 3, 3, 4, 4]
+
+
 def test_pad16():
     from plbm import pad16
     assert [pad16(n) for n in (1, 15, 16, 17, 32, 33)] == [16, 16, 16, 32, 32, 48]
