@@ -212,6 +212,33 @@ int plbm_batch_macros(plbm_batch_t *b, int grid, double *rho, double *ux, double
 /* Current lattice of grid i as binary64 f(ld,nx,0:8) on the host. */
 int plbm_batch_download(plbm_batch_t *b, int grid, double *f);
 
+/* ---- discrete adjoint -----------------------------------------------------
+ * Reverse-mode derivative of the BGK time stepper: f_0 = equilibrium(1, u0)
+ * (src/fvm_bardow.F90:99-126), nsteps x perform_lbm_step with lbm_stream +
+ * collide_bgk (src/periodic_lbm.f90:15-29), u_T = j/rho of the final state.
+ * No counterpart in the reference.  Hand-written reverse step: the Jacobian
+ * transpose of the BGK collision applied matrix-free, then streaming
+ * transposed (a push along -c_q).  Memory is bounded by checkpointing every
+ * checkpoint_every steps and recomputing each segment; dL/domega is
+ * accumulated in binary64.  storage PLBM_F64 (binary64 arithmetic) or
+ * PLBM_F32DEV (binary32 storage and per-cell arithmetic).
+ * All field pointers are DEVICE arrays of 2*nx*ny doubles: component a of
+ * cell (x,y) at a*nx*ny + y + ny*x (two (ny,nx) fields). */
+typedef struct plbm_adjoint plbm_adjoint_t;
+int plbm_adjoint_create(int nx, int ny, int storage, int nsteps, int checkpoint_every,
+                        plbm_adjoint_t **out);
+int plbm_adjoint_destroy(plbm_adjoint_t *a);
+int plbm_adjoint_set_stream(plbm_adjoint_t *a, void *cuda_stream);
+/* Device bytes held by the handle. */
+int plbm_adjoint_memory(const plbm_adjoint_t *a, size_t *bytes);
+/* Run the model from u0 with relaxation omega; writes u_T (may be NULL) and
+ * keeps the checkpoints for the next backward call.  Asynchronous. */
+int plbm_adjoint_forward(plbm_adjoint_t *a, const double *u0, double omega, double *uT);
+/* Given dL/du_T, writes dL/du0 (device, may be NULL) and dL/domega (host,
+ * may be NULL; synchronises when given). */
+int plbm_adjoint_backward(plbm_adjoint_t *a, const double *grad_uT, double *grad_u0,
+                          double *grad_omega);
+
 /* ---- raw device launches (device-resident callers: batched, autograd) ---- */
 /* One fused pull-stream + collide step over device lattices fsrc -> fdst
  * (layout above, PLBM_F64 storage = double, F32DEV = float, F16DEV = half). */

@@ -66,6 +66,8 @@ def lib(fast: bool = False) -> C.CDLL:
             "oref_sim_slbm_steps": (None, [i, i, vp, vp, d, i]),
             "oref_sim_norm": (d, [i, i, vp, vp]),
             "oref_num_threads": (i, []),
+            "oref_adjoint_bgk": (None, [i, i, vp, vp, d, i, vp, vp, vp, vp, vp, vp, vp]),
+            "oref_forward_bgk": (None, [i, i, vp, vp, d, i, vp, vp]),
         }
         for n, (r, a) in sig.items():
             fn = getattr(L, n)
@@ -216,6 +218,26 @@ def sim_slbm_steps(f1: np.ndarray, omega: float, nsteps: int) -> np.ndarray:
     b = f1.copy()
     lib().oref_sim_slbm_steps(nx, ny, _p(a), _p(b), omega, nsteps)
     return a
+
+
+def forward_bgk(ux0, uy0, omega: float, nsteps: int):
+    """u_T of f_0 = feq(1, u0) advanced nsteps BGK steps; fields (nx, ny)."""
+    ux0, uy0 = (np.ascontiguousarray(a, dtype=np.float64) for a in (ux0, uy0))
+    nx, ny = ux0.shape
+    ux, uy = np.empty((nx, ny)), np.empty((nx, ny))
+    lib().oref_forward_bgk(nx, ny, _p(ux0), _p(uy0), omega, nsteps, _p(ux), _p(uy))
+    return ux, uy
+
+
+def adjoint_bgk(ux0, uy0, omega: float, nsteps: int, gux, guy):
+    """(u_T, dL/du0, dL/domega) for a loss with dL/du_T = (gux, guy)."""
+    ux0, uy0, gux, guy = (np.ascontiguousarray(a, dtype=np.float64) for a in (ux0, uy0, gux, guy))
+    nx, ny = ux0.shape
+    out = [np.empty((nx, ny)) for _ in range(4)]
+    dom = C.c_double()
+    lib().oref_adjoint_bgk(nx, ny, _p(ux0), _p(uy0), omega, nsteps, _p(gux), _p(guy),
+                           *[_p(a) for a in out], C.addressof(dom))
+    return (out[0], out[1]), (out[2], out[3]), dom.value
 
 
 def num_threads(fast: bool = False) -> int:

@@ -771,3 +771,128 @@ double oref_sim_norm(int nx, int ny, const double *u, const double *ua)
     }
     return sqrt(a) / sqrt(b);
 }
+
+/* ------------------------------------------------------------------------ */
+/* Discrete adjoint of f_{n+1} = C(S(f_n)) (S = lbm_stream, C = collide_bgk),  */
+/* f_0 = equilibrium(1, u0), u_T = j/rho of f_T.  New code, no reference      */
+/* counterpart: the FP64 CPU check of the GPU adjoint.                        */
+static const int CXA[9] = {0, 1, 0, -1, 0, 1, -1, -1, 1};
+static const int CYA[9] = {0, 0, 1, 0, -1, 1, 1, -1, -1};
+static const double WA[9] = {4.0 / 9.0, 1.0 / 9.0, 1.0 / 9.0, 1.0 / 9.0, 1.0 / 9.0,
+                             1.0 / 36.0, 1.0 / 36.0, 1.0 / 36.0, 1.0 / 36.0};
+
+static void moments_u(const double g[9], double *rho, double *ux, double *uy)
+{
+    double r = 0.0, jx = 0.0, jy = 0.0;
+    for (int q = 0; q < 9; q++) {
+        r += g[q];
+        jx += CXA[q] * g[q];
+        jy += CYA[q] * g[q];
+    }
+    *rho = r;
+    *ux = jx / r;
+    *uy = jy / r;
+}
+
+static double *adj_states(int nx, int ny, const double *ux0, const double *uy0, double omega, int nsteps)
+{
+    int ld = oref_pad16(ny);
+    size_t lat = (size_t)ld * (size_t)nx * 9u;
+    double *F = calloc(lat * (size_t)(nsteps + 1), sizeof(double));
+    double *one = malloc(sizeof(double) * (size_t)nx * (size_t)ny);
+    for (size_t i = 0; i < (size_t)nx * (size_t)ny; i++) one[i] = 1.0;
+    oref_set_pdf_to_equilibrium(nx, ny, ld, one, ux0, uy0, F);
+    free(one);
+    for (int n = 0; n < nsteps; n++) {
+        oref_lbm_stream(nx, ny, ld, F + lat * (size_t)n, F + lat * (size_t)(n + 1));
+        oref_collide_bgk(nx, ny, ld, F + lat * (size_t)(n + 1), omega, 0);
+    }
+    return F;
+}
+
+void oref_forward_bgk(int nx, int ny, const double *ux0, const double *uy0, double omega, int nsteps,
+                      double *uxT, double *uyT)
+{
+    int ld = oref_pad16(ny);
+    size_t lat = (size_t)ld * (size_t)nx * 9u;
+    double *F = adj_states(nx, ny, ux0, uy0, omega, nsteps);
+    const double *f = F + lat * (size_t)nsteps;
+    for (int x = 0; x < nx; x++)
+        for (int y = 0; y < ny; y++) {
+            double g[9], r;
+            for (int q = 0; q < 9; q++) g[q] = f[IDX(y, x, q)];
+            size_t o = (size_t)y + (size_t)ny * (size_t)x;
+            moments_u(g, &r, &uxT[o], &uyT[o]);
+        }
+    free(F);
+}
+
+void oref_adjoint_bgk(int nx, int ny, const double *ux0, const double *uy0, double omega, int nsteps,
+                      const double *gux, const double *guy, double *uxT, double *uyT,
+                      double *grad_ux0, double *grad_uy0, double *grad_omega)
+{
+    int ld = oref_pad16(ny);
+    size_t lat = (size_t)ld * (size_t)nx * 9u;
+    double *F = adj_states(nx, ny, ux0, uy0, omega, nsteps);
+    double *lam = calloc(lat, sizeof(double)), *nxt = calloc(lat, sizeof(double));
+    /* lambda_T = dL/df_T = sum_a G_a (c_qa - u_a) / rho */
+    const double *fT = F + lat * (size_t)nsteps;
+    for (int x = 0; x < nx; x++)
+        for (int y = 0; y < ny; y++) {
+            double g[9], r, u, v;
+            for (int q = 0; q < 9; q++) g[q] = fT[IDX(y, x, q)];
+            size_t o = (size_t)y + (size_t)ny * (size_t)x;
+            moments_u(g, &r, &u, &v);
+            uxT[o] = u;
+            uyT[o] = v;
+            for (int q = 0; q < 9; q++)
+                lam[IDX(y, x, q)] = (gux[o] * (CXA[q] - u) + guy[o] * (CYA[q] - v)) / r;
+        }
+    double dom = 0.0;
+    double *g = malloc(sizeof(double) * lat);
+    for (int n = nsteps - 1; n >= 0; n--) {
+        oref_lbm_stream(nx, ny, ld, F + lat * (size_t)n, g);
+        memset(nxt, 0, sizeof(double) * lat);
+        for (int x = 0; x < nx; x++)
+            for (int y = 0; y < ny; y++) {
+                double gg[9], feq[9], l[9], r, u, v;
+                for (int q = 0; q < 9; q++) {
+                    gg[q] = g[IDX(y, x, q)];
+                    l[q] = lam[IDX(y, x, q)];
+                }
+                moments_u(gg, &r, &u, &v);
+                oref_equilibrium(r, u, v, feq);
+                double s0 = 0.0, A = 0.0, Bx = 0.0, By = 0.0, uu = u * u + v * v;
+                for (int q = 0; q < 9; q++) {
+                    dom += l[q] * (feq[q] - gg[q]);
+                    double cu = CXA[q] * u + CYA[q] * v, wl = WA[q] * l[q];
+                    s0 += wl;
+                    A += wl * (1.0 - 4.5 * cu * cu + 1.5 * uu);
+                    Bx += wl * (3.0 + 9.0 * cu) * CXA[q];
+                    By += wl * (3.0 + 9.0 * cu) * CYA[q];
+                }
+                double ex = Bx - 3.0 * s0 * u, ey = By - 3.0 * s0 * v;
+                for (int p = 0; p < 9; p++) {
+                    double mu = (1.0 - omega) * l[p] + omega * (A + CXA[p] * ex + CYA[p] * ey);
+                    int xs = (x - CXA[p] + nx) % nx, ys = (y - CYA[p] + ny) % ny; /* push along -c_p */
+                    nxt[IDX(ys, xs, p)] = mu;
+                }
+            }
+        double *t = lam; lam = nxt; nxt = t;
+    }
+    /* dL/du0 through f_0 = feq(1, u0) */
+    for (int x = 0; x < nx; x++)
+        for (int y = 0; y < ny; y++) {
+            size_t o = (size_t)y + (size_t)ny * (size_t)x;
+            double u = ux0[o], v = uy0[o], ax = 0.0, ay = 0.0;
+            for (int q = 0; q < 9; q++) {
+                double cu = CXA[q] * u + CYA[q] * v, wl = WA[q] * lam[IDX(y, x, q)];
+                ax += wl * (3.0 * CXA[q] + 9.0 * cu * CXA[q] - 3.0 * u);
+                ay += wl * (3.0 * CYA[q] + 9.0 * cu * CYA[q] - 3.0 * v);
+            }
+            grad_ux0[o] = ax;
+            grad_uy0[o] = ay;
+        }
+    *grad_omega = dom;
+    free(g); free(lam); free(nxt); free(F);
+}

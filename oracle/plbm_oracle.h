@@ -85,6 +85,19 @@ void oref_sim_slbm_steps(int nx, int ny, double *f1, double *f2, double omega, i
 /* sim/sim_slbm.F90:221-228 */
 double oref_sim_norm(int nx, int ny, const double *u, const double *ua);
 
+/* ---- discrete adjoint of the BGK time stepper (no reference counterpart) --
+ * Model: f_0 = equilibrium(1, u0) (src/fvm_bardow.F90:99-126), then nsteps of
+ * perform_lbm_step with lbm_stream + collide_bgk; u_T = j/rho of the final
+ * state.  Given G = dL/du_T (arrays gux, guy of shape (ny,nx)), returns
+ * dL/du0 (arrays (ny,nx)) and dL/domega, by reverse-mode differentiation of
+ * every step (all states kept: small grids only).  Also writes u_T. */
+void oref_adjoint_bgk(int nx, int ny, const double *ux0, const double *uy0, double omega, int nsteps,
+                      const double *gux, const double *guy, double *uxT, double *uyT,
+                      double *grad_ux0, double *grad_uy0, double *grad_omega);
+/* Forward only: u_T of the same model. */
+void oref_forward_bgk(int nx, int ny, const double *ux0, const double *uy0, double omega, int nsteps,
+                      double *uxT, double *uyT);
+
 /* ---- OpenMP thread count actually used (for the CPU baseline report) ---- */
 int oref_num_threads(void);
 

@@ -36,6 +36,7 @@ UNITS = [
     ("grid.cpp", "grid.o", ["-x", "cu", "--fmad=false"]),
     ("plugin.cpp", "plugin.o", ["-x", "cu", "--fmad=false"]),
     ("batch.cpp", "batch.o", ["-x", "cu", "--fmad=false"]),
+    ("adjoint.cpp", "adjoint_host.o", ["-x", "cu", "--fmad=false"]),
 ]
 
 

@@ -1,0 +1,231 @@
+// adjoint.cpp -- plbm_adjoint_* C ABI: forward run with checkpoints and the
+// reverse sweep with recomputation (sqrt(T) memory), see adjoint.cu.
+//
+// Checkpoints hold f_n for n = 0, K, 2K, ... (K = checkpoint_every).  The
+// reverse sweep walks the segments [kK, min(kK+K, T)) from the last: it
+// recomputes the segment's states from checkpoint k into a K-lattice buffer,
+// then applies the reverse steps n = end-1 .. kK.  Device memory:
+// (ceil(T/K) + K + 4) lattices.  Each forward step is computed twice in all
+// (forward pass + recomputation).
+#include <cuda_runtime.h>
+#include <string.h>
+#include <vector>
+
+#include "../../include/plbm_gpu.h"
+#include "plbm_adjoint.h"
+#include "plbm_launch.h"
+
+namespace plbm_internal {
+int fail(int code, const char* fmt, ...);
+int cuda_fail(cudaError_t e, const char* what);
+}  // namespace plbm_internal
+using plbm_internal::cuda_fail;
+using plbm_internal::fail;
+using namespace plbm;
+CollParams plbm_make_params(double omega, double trt_magic);
+
+#define CUDA_TRY(expr, what)                            \
+  do {                                                  \
+    cudaError_t e_ = (expr);                            \
+    if (e_ != cudaSuccess) return cuda_fail(e_, what);  \
+  } while (0)
+
+struct plbm_adjoint {
+  int nx, ny, ld, storage, nsteps, K, nck, device;
+  size_t lat_bytes;
+  char* ck = nullptr;    // nck lattices
+  char* seg = nullptr;   // K lattices
+  char* work = nullptr;  // 2 lattices
+  char* lam = nullptr;   // 2 lattices
+  double* u0 = nullptr;  // 2*nx*ny
+  double* dom = nullptr; // adjoint_blocks slots
+  int nblocks = 0;
+  double omega = 1.0;
+  const void* fT = nullptr;
+  int have_forward = 0;
+  cudaStream_t own = nullptr, stream = nullptr;
+};
+
+namespace {
+
+int pad16(int n) { return n % 16 ? n + (16 - n % 16) : n; }
+
+void* lat(char* base, const plbm_adjoint_t* a, int i) { return base + (size_t)i * a->lat_bytes; }
+
+cudaError_t fwd_step(const plbm_adjoint_t* a, const void* src, void* dst, const CollParams& p) {
+  Sweep s{a->nx, a->ny, a->ld, src, dst, a->stream};
+  if (a->storage == PLBM_F64) return fma::step_pull_f64(K_BGK, s, p);
+  return step_pull_dev(ST_F32DEV, K_BGK, s, p);
+}
+
+AdjLaunch base_launch(const plbm_adjoint_t* a) {
+  AdjLaunch L;
+  memset(&L, 0, sizeof L);
+  L.nx = a->nx;
+  L.ny = a->ny;
+  L.ld = a->ld;
+  L.omega = a->omega;
+  L.stream = a->stream;
+  return L;
+}
+
+int st(const plbm_adjoint_t* a) { return a->storage == PLBM_F64 ? ST_F64 : ST_F32DEV; }
+
+}  // namespace
+
+extern "C" int plbm_adjoint_create(int nx, int ny, int storage, int nsteps, int checkpoint_every,
+                                   plbm_adjoint_t** out) {
+  if (!out) return fail(PLBM_E_INVALID, "out is NULL");
+  *out = nullptr;
+  if (nx < 1 || ny < 1 || nsteps < 1 || checkpoint_every < 1)
+    return fail(PLBM_E_INVALID, "bad adjoint sizes nx=%d ny=%d nsteps=%d checkpoint_every=%d", nx, ny, nsteps,
+                checkpoint_every);
+  if (storage != PLBM_F64 && storage != PLBM_F32DEV)
+    return fail(PLBM_E_UNSUPPORTED, "adjoint storage %d (PLBM_F64 or PLBM_F32DEV)", storage);
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+    cudaGetLastError();
+    return fail(PLBM_E_NODEVICE, "no CUDA device visible");
+  }
+  plbm_adjoint_t* a = new plbm_adjoint_t();
+  a->nx = nx;
+  a->ny = ny;
+  a->ld = pad16(ny);
+  a->storage = storage;
+  a->nsteps = nsteps;
+  a->K = checkpoint_every < nsteps ? checkpoint_every : nsteps;
+  a->nck = (nsteps + a->K - 1) / a->K;
+  cudaGetDevice(&a->device);
+  a->lat_bytes = (size_t)a->ld * nx * 9 * (storage == PLBM_F64 ? 8 : 4);
+  a->nblocks = adjoint_blocks(nx, ny);
+  cudaError_t e = cudaMalloc(&a->ck, a->lat_bytes * a->nck);
+  if (e == cudaSuccess) e = cudaMalloc(&a->seg, a->lat_bytes * a->K);
+  if (e == cudaSuccess) e = cudaMalloc(&a->work, a->lat_bytes * 2);
+  if (e == cudaSuccess) e = cudaMalloc(&a->lam, a->lat_bytes * 2);
+  if (e == cudaSuccess) e = cudaMalloc(&a->u0, sizeof(double) * 2 * (size_t)nx * ny);
+  if (e == cudaSuccess) e = cudaMalloc(&a->dom, sizeof(double) * a->nblocks);
+  // padding rows are never written by the kernels: give them a defined value
+  if (e == cudaSuccess) e = cudaMemset(a->ck, 0, a->lat_bytes * a->nck);
+  if (e == cudaSuccess) e = cudaMemset(a->seg, 0, a->lat_bytes * a->K);
+  if (e == cudaSuccess) e = cudaMemset(a->work, 0, a->lat_bytes * 2);
+  if (e == cudaSuccess) e = cudaMemset(a->lam, 0, a->lat_bytes * 2);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&a->own, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    plbm_adjoint_destroy(a);
+    return cuda_fail(e, "adjoint allocation");
+  }
+  a->stream = a->own;
+  *out = a;
+  return PLBM_OK;
+}
+
+extern "C" int plbm_adjoint_destroy(plbm_adjoint_t* a) {
+  if (!a) return PLBM_OK;
+  cudaSetDevice(a->device);
+  if (a->stream) cudaStreamSynchronize(a->stream);
+  cudaFree(a->ck);
+  cudaFree(a->seg);
+  cudaFree(a->work);
+  cudaFree(a->lam);
+  cudaFree(a->u0);
+  cudaFree(a->dom);
+  if (a->own) cudaStreamDestroy(a->own);
+  delete a;
+  return PLBM_OK;
+}
+
+extern "C" int plbm_adjoint_set_stream(plbm_adjoint_t* a, void* stream) {
+  if (!a) return fail(PLBM_E_INVALID, "NULL adjoint");
+  a->stream = stream ? static_cast<cudaStream_t>(stream) : a->own;
+  return PLBM_OK;
+}
+
+extern "C" int plbm_adjoint_memory(const plbm_adjoint_t* a, size_t* bytes) {
+  if (!a || !bytes) return fail(PLBM_E_INVALID, "NULL argument");
+  *bytes = a->lat_bytes * ((size_t)a->nck + a->K + 4) + sizeof(double) * (2 * (size_t)a->nx * a->ny + a->nblocks);
+  return PLBM_OK;
+}
+
+extern "C" int plbm_adjoint_forward(plbm_adjoint_t* a, const double* u0, double omega, double* uT) {
+  if (!a || !u0) return fail(PLBM_E_INVALID, "NULL argument");
+  if (!(omega > 0.0 && omega < 2.0)) return fail(PLBM_E_INVALID, "omega = %g outside (0,2)", omega);
+  CUDA_TRY(cudaSetDevice(a->device), "cudaSetDevice");
+  const size_t n2 = 2 * (size_t)a->nx * a->ny;
+  a->omega = omega;
+  CUDA_TRY(cudaMemcpyAsync(a->u0, u0, n2 * sizeof(double), cudaMemcpyDeviceToDevice, a->stream), "copy u0");
+  AdjLaunch L = base_launch(a);
+  L.u = a->u0;
+  L.f = lat(a->ck, a, 0);
+  CUDA_TRY(adjoint_launch(st(a), 0, L), "adjoint init kernel");
+  const CollParams p = plbm_make_params(omega, 0.25);
+  const void* cur = lat(a->ck, a, 0);
+  int tog = 0;
+  for (int n = 0; n < a->nsteps; n++) {
+    void* dst = lat(a->work, a, tog);
+    tog ^= 1;
+    CUDA_TRY(fwd_step(a, cur, dst, p), "forward step");
+    cur = dst;
+    if ((n + 1) % a->K == 0 && (n + 1) < a->nsteps)
+      CUDA_TRY(cudaMemcpyAsync(lat(a->ck, a, (n + 1) / a->K), cur, a->lat_bytes, cudaMemcpyDeviceToDevice, a->stream),
+               "checkpoint copy");
+  }
+  a->fT = cur;
+  if (uT) {
+    L = base_launch(a);
+    L.f = a->fT;
+    L.out = uT;
+    CUDA_TRY(adjoint_launch(st(a), 1, L), "final moments kernel");
+  }
+  a->have_forward = 1;
+  return PLBM_OK;
+}
+
+extern "C" int plbm_adjoint_backward(plbm_adjoint_t* a, const double* grad_uT, double* grad_u0,
+                                     double* grad_omega) {
+  if (!a || !grad_uT) return fail(PLBM_E_INVALID, "NULL argument");
+  if (!a->have_forward) return fail(PLBM_E_INVALID, "plbm_adjoint_backward before plbm_adjoint_forward");
+  CUDA_TRY(cudaSetDevice(a->device), "cudaSetDevice");
+  AdjLaunch L = base_launch(a);
+  L.f = a->fT;
+  L.g = grad_uT;
+  L.lam_out = lat(a->lam, a, 0);
+  CUDA_TRY(adjoint_launch(st(a), 1, L), "lambda_T kernel");
+  CUDA_TRY(cudaMemsetAsync(a->dom, 0, sizeof(double) * a->nblocks, a->stream), "clear domega");
+  const CollParams p = plbm_make_params(a->omega, 0.25);
+  int li = 0;
+  for (int k = a->nck - 1; k >= 0; k--) {
+    const int n0 = k * a->K;
+    const int n1 = n0 + a->K < a->nsteps ? n0 + a->K : a->nsteps;
+    // recompute f_{n0+1} .. f_{n1-1} into seg[1..]
+    for (int i = 1; i < n1 - n0; i++) {
+      const void* src = i == 1 ? lat(a->ck, a, k) : lat(a->seg, a, i - 1);
+      CUDA_TRY(fwd_step(a, src, lat(a->seg, a, i), p), "recompute step");
+    }
+    for (int n = n1 - 1; n >= n0; n--) {
+      L = base_launch(a);
+      L.f = n == n0 ? lat(a->ck, a, k) : lat(a->seg, a, n - n0);
+      L.lam_in = lat(a->lam, a, li);
+      L.lam_out = lat(a->lam, a, 1 - li);
+      L.dom = a->dom;
+      CUDA_TRY(adjoint_launch(st(a), 2, L), "reverse step");
+      li = 1 - li;
+    }
+  }
+  if (grad_u0) {
+    L = base_launch(a);
+    L.lam_in = lat(a->lam, a, li);
+    L.u = a->u0;
+    L.out = grad_u0;
+    CUDA_TRY(adjoint_launch(st(a), 3, L), "dL/du0 kernel");
+  }
+  if (grad_omega) {
+    std::vector<double> h(a->nblocks);
+    CUDA_TRY(cudaMemcpyAsync(h.data(), a->dom, sizeof(double) * a->nblocks, cudaMemcpyDeviceToHost, a->stream),
+             "download domega");
+    CUDA_TRY(cudaStreamSynchronize(a->stream), "adjoint sync");
+    double s = 0.0;
+    for (int b = 0; b < a->nblocks; b++) s += h[b];
+    *grad_omega = s;
+  }
+  return PLBM_OK;
+}

@@ -105,6 +105,13 @@ SIGNATURES = {
     "plbm_batch_steps": (C.c_int, [_vp, C.POINTER(C.c_longlong)]),
     "plbm_batch_macros": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp]),
     "plbm_batch_download": (C.c_int, [_vp, C.c_int, _vp]),
+    # adjoint
+    "plbm_adjoint_create": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(_vp)]),
+    "plbm_adjoint_destroy": (C.c_int, [_vp]),
+    "plbm_adjoint_set_stream": (C.c_int, [_vp, _vp]),
+    "plbm_adjoint_memory": (C.c_int, [_vp, C.POINTER(C.c_size_t)]),
+    "plbm_adjoint_forward": (C.c_int, [_vp, _vp, C.c_double, _vp]),
+    "plbm_adjoint_backward": (C.c_int, [_vp, _vp, _vp, _dp]),
     # plugin ABI (include/plbm_plugin.h)
     "c_plbmgpu_init": (_vp, [C.c_int, C.c_int, C.c_double, _vp, _vp, _vp, _vp]),
     "c_plbmgpu_step": (None, [_vp, C.c_double]),
@@ -155,6 +162,23 @@ def check(code: int) -> int:
     if code < 0:
         raise PlbmError(code, last_error())
     return code
+
+
+CUDA_STREAM_LEGACY = 0x1  # cudaStreamLegacy
+
+
+def stream_handle(stream) -> int | None:
+    """cudaStream_t value for a torch stream / raw handle.
+
+    torch reports the legacy default stream as 0, which the plbm_* entry points
+    read as "the handle's own stream"; it is passed as cudaStreamLegacy so the
+    library's work is ordered with torch's default-stream work.  None keeps the
+    handle's own stream.
+    """
+    if stream is None:
+        return None
+    s = getattr(stream, "cuda_stream", stream)
+    return int(s) if s else CUDA_STREAM_LEGACY
 
 
 def ptr(a) -> int | None:

@@ -113,7 +113,8 @@ class BatchedGrids:
         check(self._lib.plbm_batch_set_schedule(self._h, C.addressof(s)))
 
     def set_stream(self, stream) -> None:
-        s = getattr(stream, "cuda_stream", stream)
+        """torch stream or raw cudaStream_t; None = the batch's own stream."""
+        s = _lib.stream_handle(stream)
         check(self._lib.plbm_batch_set_stream(self._h, C.c_void_p(s) if s else None))
 
     # -- state ------------------------------------------------------------------

@@ -141,8 +141,10 @@ class LatticeGrid:
         return self.indices[1]
 
     def set_stream(self, stream) -> None:
-        """Queue the handle's work on a cudaStream_t (int handle, torch stream, or None)."""
-        s = getattr(stream, "cuda_stream", stream)
+        """Queue the handle's work on a torch stream or raw cudaStream_t; None = own stream.
+
+        torch's legacy default stream (handle 0) maps to cudaStreamLegacy."""
+        s = _lib.stream_handle(stream)
         check(self._lib.plbm_grid_set_stream(self.handle, C.c_void_p(s) if s else None))
 
     def device_ptr(self, ibuf: int) -> int:

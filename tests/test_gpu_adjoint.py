@@ -1,0 +1,126 @@
+"""GPU tests of the discrete adjoint and its torch.autograd.Function:
+against the FP64 CPU adjoint, against central finite differences of the
+binary64 model, invariance under the checkpoint interval, and the binary32
+deviation-storage adjoint against the binary64 one."""
+import math
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def fields(nx, ny, seed=3, amp=0.01):
+    from plbm import cases
+    ux, uy = cases.divergence_free_modes(max(nx, ny), nmodes=8, kmax=4, amp=amp, seed=seed)
+    return np.ascontiguousarray(ux[:nx, :ny]), np.ascontiguousarray(uy[:nx, :ny])
+
+
+def test_gpu_adjoint_matches_cpu_adjoint(gpu_lib):
+    import torch
+    from plbm.autograd import Adjoint
+    nx, ny, steps, omega = 40, 28, 60, 1.4
+    ux0, uy0 = fields(nx, ny)
+    tx, ty = fields(nx, ny, seed=5)
+    (uT, vT) = O.forward_bgk(ux0, uy0, omega, steps)
+    _, (gx, gy), gom = O.adjoint_bgk(ux0, uy0, omega, steps, uT - tx, vT - ty)
+    a = Adjoint(nx, ny, steps, checkpoint_every=7, storage="f64")
+    u0 = torch.tensor(np.stack([ux0, uy0]), device="cuda")
+    uTg = a.forward(u0, omega)
+    got_uT = uTg.cpu().numpy()
+    assert np.max(np.abs(got_uT[0] - uT)) <= 1e-12 * np.max(np.abs(uT))
+    G = uTg - torch.tensor(np.stack([tx, ty]), device="cuda")
+    g0, dom = a.backward(G)
+    g0 = g0.cpu().numpy()
+    scale = np.max(np.abs(np.stack([gx, gy])))
+    assert np.max(np.abs(g0[0] - gx)) <= 1e-9 * scale
+    assert np.max(np.abs(g0[1] - gy)) <= 1e-9 * scale
+    assert abs(dom - gom) <= 1e-9 * abs(gom)
+    a.close()
+
+
+def test_checkpoint_interval_does_not_change_gradients(gpu_lib):
+    import torch
+    from plbm.autograd import Adjoint
+    nx, ny, steps = 33, 20, 50
+    ux0, uy0 = fields(nx, ny)
+    u0 = torch.tensor(np.stack([ux0, uy0]), device="cuda")
+    res = []
+    for k in (1, 7, 50, 13):
+        a = Adjoint(nx, ny, steps, checkpoint_every=k)
+        uT = a.forward(u0, 1.2)
+        g, dom = a.backward(uT)  # loss 0.5 |u_T|^2
+        res.append((g.cpu().numpy(), dom))
+        a.close()
+    for g, dom in res[1:]:
+        assert np.array_equal(g, res[0][0]) and dom == res[0][1]
+
+
+def test_autograd_against_central_differences(gpu_lib):
+    """dL/du0 and dL/dtau of L = 1/2 |u_T - u*|^2 by the adjoint vs central
+    differences (h = 1e-4 relative) of the binary64 forward model."""
+    import torch
+    from plbm.autograd import lbm_final_velocity, velocity_misfit
+    nx = ny = 48
+    steps = 120
+    ux0, uy0 = fields(nx, ny, seed=1)
+    tx, ty = fields(nx, ny, seed=2)
+    u0 = torch.tensor(np.stack([ux0, uy0]), device="cuda", requires_grad=True)
+    tau = torch.tensor(0.8, dtype=torch.float64, device="cuda", requires_grad=True)
+    target = torch.tensor(np.stack([tx, ty]), device="cuda")
+    L = velocity_misfit(u0, tau, target, steps, checkpoint_every=11)
+    L.backward()
+    gu = u0.grad.cpu().numpy()
+
+    def loss(u, t):
+        with torch.no_grad():
+            return float(0.5 * torch.sum((lbm_final_velocity(u, t, steps) - target) ** 2))
+
+    rng = np.random.default_rng(0)
+    scale = np.max(np.abs(gu))
+    for _ in range(8):
+        a, i, j = int(rng.integers(2)), int(rng.integers(nx)), int(rng.integers(ny))
+        h = 1e-4 * max(abs(float(u0[a, i, j])), 1e-3)
+        up = u0.detach().clone()
+        um = u0.detach().clone()
+        up[a, i, j] += h
+        um[a, i, j] -= h
+        fd = (loss(up, 0.8) - loss(um, 0.8)) / (2 * h)
+        assert abs(fd - gu[a, i, j]) <= 1e-5 * scale, (a, i, j, fd, gu[a, i, j])
+    h = 1e-4 * 0.8
+    fd_tau = (loss(u0.detach(), 0.8 + h) - loss(u0.detach(), 0.8 - h)) / (2 * h)
+    assert abs(fd_tau - float(tau.grad)) <= 1e-5 * abs(fd_tau)
+
+
+def test_f32_adjoint_close_to_f64_adjoint(gpu_lib):
+    import torch
+    from plbm.autograd import Adjoint
+    nx, ny, steps = 64, 64, 100
+    ux0, uy0 = fields(nx, ny, seed=7)
+    tx, ty = fields(nx, ny, seed=8)
+    u0 = torch.tensor(np.stack([ux0, uy0]), device="cuda")
+    tgt = torch.tensor(np.stack([tx, ty]), device="cuda")
+    out = {}
+    for st in ("f64", "f32dev"):
+        a = Adjoint(nx, ny, steps, checkpoint_every=10, storage=st)
+        uT = a.forward(u0, 1.25)
+        out[st] = a.backward(uT - tgt)
+        a.close()
+    g64, d64 = out["f64"]
+    g32, d32 = out["f32dev"]
+    rel = float(torch.linalg.norm(g32 - g64) / torch.linalg.norm(g64))
+    print(f"f32dev vs f64 adjoint: dL/du0 relative L2 {rel:.2e}, dL/domega rel {abs(d32 - d64) / abs(d64):.2e}")
+    assert rel < 1e-3
+    assert abs(d32 - d64) <= 1e-3 * abs(d64)
+
+
+def test_adjoint_errors(gpu_lib):
+    from plbm import PlbmError
+    from plbm.autograd import Adjoint
+    import torch
+    a = Adjoint(16, 16, 10)
+    with pytest.raises(PlbmError):
+        a.backward(torch.zeros((2, 16, 16), dtype=torch.float64, device="cuda"))  # no forward yet
+    a.close()

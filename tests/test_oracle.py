@@ -165,6 +165,33 @@ def test_taylor_green_decay_64():
     assert O.tgv_l2_norm(u, v, uxa, uya) < 5e-3
 
 
+def test_cpu_adjoint_matches_central_differences():
+    """The FP64 CPU adjoint (the check for the GPU adjoint) against central
+    finite differences of the same forward model, loss 0.5 |u_T - u*|^2."""
+    nx, ny, steps, omega = 12, 10, 25, 1.3
+    rng = np.random.default_rng(9)
+    ux0, uy0 = 0.02 * rng.standard_normal((2, nx, ny))
+    tx, ty = 0.01 * rng.standard_normal((2, nx, ny))
+
+    def loss(u, v, om):
+        a, b = O.forward_bgk(u, v, om, steps)
+        return 0.5 * np.sum((a - tx) ** 2 + (b - ty) ** 2)
+
+    (uT, vT) = O.forward_bgk(ux0, uy0, omega, steps)
+    _, (gx, gy), gom = O.adjoint_bgk(ux0, uy0, omega, steps, uT - tx, vT - ty)
+    h = 1e-6
+    for (i, j, comp) in [(0, 0, 0), (3, 7, 1), (11, 9, 0), (5, 2, 1), (7, 4, 0)]:
+        up, vp_ = ux0.copy(), uy0.copy()
+        um, vm = ux0.copy(), uy0.copy()
+        (up if comp == 0 else vp_)[i, j] += h
+        (um if comp == 0 else vm)[i, j] -= h
+        fd = (loss(up, vp_, omega) - loss(um, vm, omega)) / (2 * h)
+        ad = (gx if comp == 0 else gy)[i, j]
+        assert abs(fd - ad) <= 1e-6 * max(abs(ad), 1e-3 * np.max(np.abs(gx)))
+    fd_om = (loss(ux0, uy0, omega + h) - loss(ux0, uy0, omega - h)) / (2 * h)
+    assert abs(fd_om - gom) <= 1e-6 * abs(gom)
+
+
 def test_taylor_green_reference_loop_quirk():
     """The reference TGV loop runs y = 1..nx; on nx == ny both loops agree."""
     a = O.taylor_green(8, 8, 0.7, 0.7, 0.01, 0.1, ref_loop=True)
