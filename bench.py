@@ -1,19 +1,26 @@
 """Benchmark of the D2Q9 periodic stream-collide hot path on GB300.
 
-Workload (default): plain single-grid bandwidth bench, D2Q9 BGK, tau = 0.6,
+Headline workload: plain single-grid bandwidth bench, D2Q9 BGK, tau = 0.6,
 8192 x 8192 periodic grid, binary64 SoA f(ld,nx,0:8), two lattices (9.66 GB,
-far larger than the 129 MB L2, so no L2 flush is needed between steps).
-Initial state: Taylor-Green vortex u0 = 0.05 (k = 2 pi / 8192) plus seeded
-i.i.d. N(0, 1e-4^2) velocity noise, f at equilibrium.  A step is one
+75x the 129 MB L2, so no L2 flush is needed between steps).  Initial state:
+Taylor-Green vortex u0 = 0.05 (k = 2 pi / 8192) plus seeded i.i.d.
+N(0, 1e-4^2) velocity noise, f at equilibrium.  A step is one
 perform_lbm_step (one fused pull-stream + collide kernel) over the grid.
+The headline arithmetic is PLBM_MATH_HYBRID (binary64 storage and final
+FMAs, exact integer moments; see DESIGN notes in the package); the straight
+binary64 kernel is measured beside it ("variants.fp64_native").
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                     [--n 8192] [--kind bgk|trt|rr] [--storage f64|f32dev|f16dev]
-                    [--math fma|strict|hybrid]
+                    [--math fma|strict|hybrid] [--no-variants] [--no-cpu-baseline]
+                    [--suite mixed]
 
 Prints one JSON line (rank 0).  --impl reference times the reference's
 algorithm on the host cores instead: the C restatement of the Fortran
 (two passes per step, stream then collide, OpenMP over all host threads).
+--suite mixed runs the mixed-precision study (shear layer, 8192^2, tau 0.52,
+velocity L2 error of binary32/binary16 deviation storage against binary64 at
+steps 1000/5000/20000) and prints its own JSON line.
 """
 from __future__ import annotations
 
@@ -40,8 +47,9 @@ import numpy as np  # noqa: E402
 # populations) by storage.
 BYTES_PER_CELL = {"f64": 144, "f32dev": 72, "f16dev": 36}
 # DRAM bytes per cell update measured by ncu (dram__bytes_read.sum +
-# dram__bytes_write.sum of one launch / cells), from profiles/.  None: no capture yet.
-NCU_TRAFFIC_PER_CELL = {}
+# dram__bytes_write.sum of one launch / cells) on a 2048^2 capture of the same
+# kernel, scaled by the cell count: profiles/k_step_*_2048_fullset.md.
+NCU_TRAFFIC_PER_CELL = {("f64", "bgk", "hybrid"): 132.7, ("f64", "bgk", "fma"): 132.4}
 FALLBACK_HBM_GBS = 6800.0
 
 
@@ -147,6 +155,17 @@ def cpu_model() -> str:
     return "unknown"
 
 
+def workload_config(args) -> dict:
+    esize = {"f64": 8, "f32dev": 4, "f16dev": 2}[args.storage]
+    return {"workload": f"plain single-grid bandwidth bench: D2Q9 {args.kind.upper()} tau={args.tau} "
+                        f"{args.n}x{args.n} periodic, {args.storage} SoA two-lattice, TGV u0=0.05 + N(0,1e-4^2) noise",
+            "grid": [args.n, args.n], "collision": args.kind, "tau": args.tau, "storage": args.storage,
+            "math": args.math, "layout": "f(ld,nx,0:8) y-fastest, ld=pad16(ny)",
+            "l2_policy": f"inputs larger than L2 (two lattices of {2 * 9 * args.n * args.n * esize / 1e9:.2f} GB "
+                         "vs 129 MB L2); no flush",
+            "parallelism": f"replicas x{args.gpus}" if args.gpus > 1 else "single GPU"}
+
+
 def run_reference(args) -> None:
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -171,15 +190,113 @@ def run_reference(args) -> None:
     print(json.dumps(line), flush=True)
 
 
-def workload_config(args) -> dict:
-    return {"workload": f"plain single-grid bandwidth bench: D2Q9 {args.kind.upper()} tau={args.tau} "
-                        f"{args.n}x{args.n} periodic, {args.storage} SoA two-lattice, TGV u0=0.05 + N(0,1e-4^2) noise",
-            "grid": [args.n, args.n], "collision": args.kind, "tau": args.tau, "storage": args.storage,
-            "math": args.math, "layout": "f(ld,nx,0:8) y-fastest, ld=pad16(ny)",
-            "l2_policy": "inputs larger than L2 (two lattices of "
-                         f"{2 * 9 * args.n * args.n * {'f64': 8, 'f32dev': 4, 'f16dev': 2}[args.storage] / 1e9:.2f} GB"
-                         " vs 129 MB L2); no flush",
-            "parallelism": f"replicas x{args.gpus}" if args.gpus > 1 else "single GPU"}
+# ---------------------------------------------------------------------------
+def time_grid_steps(torch, n, storage, kind, math_mode, omega, steps, warmup, fields):
+    """Device-resident MLUPS of one grid configuration (CUDA events, own stream)."""
+    from plbm import LatticeGrid
+    stream = torch.cuda.Stream()
+    g = LatticeGrid(n, n, storage=storage, collision=kind, math=math_mode)
+    g.set_stream(stream.cuda_stream)
+    g.set_relaxation(omega, 0.25)
+    g.set_pdf_to_equilibrium(*fields)
+    g.perform_lbm_step(warmup)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    g.perform_lbm_step(steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    g.close()
+    return ms / steps
+
+
+def variant_entry(n, storage, ms_step, peak):
+    mlups = n * n / (ms_step * 1e-3) / 1e6
+    gbs = mlups * 1e6 * BYTES_PER_CELL[storage] / 1e9
+    return {"value": mlups, "unit": "MLUPS", "ms_per_step": ms_step, "achieved_gbs": gbs, "frac_hbm": gbs / peak,
+            "bytes_per_cell": BYTES_PER_CELL[storage]}
+
+
+MIXED_CONFS = (("f32dev", "hybrid"), ("f32dev", "fma"), ("f16dev", "hybrid"), ("f16dev", "fma"))
+
+
+def mixed_precision_errors(torch, n, tau, checkpoints):
+    """Velocity L2 error of binary32/binary16 deviation storage (compensated
+    "hybrid" and plain binary32 collision) against the binary64 run, shear
+    layer k=80, delta=0.05, u0=0.04, BGK tau."""
+    from plbm import LatticeGrid, cases
+    rho, ux, uy = cases.shear_layer(n, n, float(n), 0.04, 80.0, 0.05)
+    grids = {}
+    for st, mm in (("f64", "hybrid"),) + MIXED_CONFS:
+        g = LatticeGrid(n, n, storage=st, collision="bgk", math=mm)
+        g.set_relaxation(1.0 / tau, 0.25)
+        g.set_pdf_to_equilibrium(rho, ux, uy)
+        grids[(st, mm)] = g
+    out = {f"{st}/{mm}": {} for st, mm in MIXED_CONFS}
+    done = 0
+    for c in checkpoints:
+        for g in grids.values():
+            g.perform_lbm_step(c - done)
+        done = c
+        _, u64, v64 = grids[("f64", "hybrid")].update_macros()
+        den = float(np.sum(u64 * u64 + v64 * v64))
+        for st, mm in MIXED_CONFS:
+            _, u, v = grids[(st, mm)].update_macros()
+            out[f"{st}/{mm}"][str(c)] = math.sqrt(float(np.sum((u - u64) ** 2 + (v - v64) ** 2)) / den)
+    for g in grids.values():
+        g.close()
+    return out
+
+
+def batched_variant(torch, storage, steps):
+    from plbm import autotune, batched
+    b = batched.build_tgv_batch(512, 2024, storage)
+    _, rep = autotune.tune(b, steps=5, reps=1, use_cache=True)
+    stream = torch.cuda.Stream()
+    b.set_stream(stream.cuda_stream)
+    b.capture(steps)
+    b.launch_graph()
+    b.synchronize()
+    if b.steps % 2:
+        b.capture(steps)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    b.launch_graph()
+    e1.record(stream)
+    b.synchronize()
+    ms = e0.elapsed_time(e1)
+    cells = b.cells
+    b.close()
+    mlups = cells * steps / (ms * 1e-3) / 1e6
+    return {"value": mlups, "unit": "MLUPS", "grids": 512, "cells": cells, "steps_per_graph": steps,
+            "ms_per_step": ms / steps, "schedule": rep["schedule"], "schedule_cached": rep.get("cached", False),
+            "achieved_gbs": mlups * 1e6 * BYTES_PER_CELL[storage] / 1e9}
+
+
+def adjoint_variant(torch, storage, n=1024, T=2000, K=45):
+    from plbm import cases
+    from plbm.autograd import Adjoint
+    ux, uy = cases.divergence_free_modes(n, 16, 8, 0.01, seed=1)
+    tx, ty = cases.divergence_free_modes(n, 16, 8, 0.01, seed=2)
+    u0 = torch.tensor(np.stack([ux, uy]), device="cuda")
+    tgt = torch.tensor(np.stack([tx, ty]), device="cuda")
+    a = Adjoint(n, n, T, K, storage)
+    uT = a.forward(u0, 1 / 0.8)
+    a.backward(uT - tgt)
+    torch.cuda.synchronize()
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    e[0].record()
+    uT = a.forward(u0, 1 / 0.8)
+    e[1].record()
+    a.backward(uT - tgt)
+    e[2].record()
+    torch.cuda.synchronize()
+    f_ms, b_ms = e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2])
+    mem = a.memory_bytes()
+    a.close()
+    return {"grid": [n, n], "steps": T, "checkpoint_every": K, "forward_ms": f_ms, "backward_ms": b_ms,
+            "adjoint_over_forward": b_ms / f_ms, "device_GB": mem / 1e9}
 
 
 def main() -> None:
@@ -192,11 +309,15 @@ def main() -> None:
     ap.add_argument("--kind", default="bgk", choices=["bgk", "trt", "rr"])
     ap.add_argument("--tau", type=float, default=0.6)
     ap.add_argument("--storage", default="f64", choices=["f64", "f32dev", "f16dev"])
-    ap.add_argument("--math", default="fma", choices=["fma", "strict", "hybrid"])
+    ap.add_argument("--math", default=None, choices=["fma", "strict", "hybrid"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU-baseline sample length")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-variants", action="store_true")
+    ap.add_argument("--suite", default=None, choices=["mixed"])
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.math is None:
+        args.math = "hybrid" if (args.storage == "f64" and args.kind == "bgk") else "fma"
 
     if args.impl == "reference":
         run_reference(args)
@@ -219,6 +340,13 @@ def main() -> None:
         import __graft_entry__ as ge
         ge.build()
         _lib.load()
+
+    if args.suite == "mixed":
+        if rank == 0:
+            errs = mixed_precision_errors(torch, args.n, 0.52, (1000, 5000, 20000))
+            print(json.dumps({"suite": "mixed", "workload": f"shear layer {args.n}^2 BGK tau=0.52 k=80 delta=0.05 "
+                              "u0=0.04", "velocity_l2_vs_f64": errs}), flush=True)
+        return
 
     n, omega = args.n, 1.0 / args.tau
     fields = initial_fields(n)
@@ -285,6 +413,7 @@ def main() -> None:
     h2d = 9 * n * ld * 8
     d2h = 3 * n * n * 8
     g.close()
+    del host_f, host_m
 
     if rank != 0:
         if world > 1:
@@ -300,7 +429,7 @@ def main() -> None:
         "metric": "MLUPS", "value": mlups, "unit": "MLUPS", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": {"f64": "f64", "f32dev": "f32", "f16dev": "f16"}[args.storage] ,
+        "dtype": {"f64": "f64", "f32dev": "f32", "f16dev": "f16"}[args.storage],
         "data": "synthetic (seeded TGV + noise, no dataset)",
         "config": workload_config(args),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -312,9 +441,28 @@ def main() -> None:
         "gpu_launches": args.steps,
         "clocks": clocks,
     }
+    if not args.no_variants:
+        torch.cuda.empty_cache()
+        var = {}
+        var["fp64_native"] = variant_entry(n, "f64", time_grid_steps(torch, n, "f64", args.kind, "fma", omega, 20, 3,
+                                                                    fields), peak)
+        var["fp32dev"] = variant_entry(n, "f32dev", time_grid_steps(torch, n, "f32dev", args.kind, "fma", omega, 50, 3,
+                                                                   fields), peak)
+        if args.kind == "bgk":
+            var["fp32dev_compensated"] = variant_entry(
+                n, "f32dev", time_grid_steps(torch, n, "f32dev", "bgk", "hybrid", omega, 50, 3, fields), peak)
+        var["fp16dev"] = variant_entry(n, "f16dev", time_grid_steps(torch, n, "f16dev", args.kind, "fma", omega, 50, 3,
+                                                                   fields), peak)
+        mp = mixed_precision_errors(torch, n, 0.52, (1000,))
+        var["mixed_precision_l2_vs_f64"] = {
+            "workload": f"shear layer {n}^2 BGK tau=0.52 k=80 delta=0.05 u0=0.04, step 1000 "
+                        "(steps 5000/20000: bench.py --suite mixed)", **mp}
+        var["batched_f64"] = batched_variant(torch, "f64", 50)
+        var["batched_f32dev"] = batched_variant(torch, "f32dev", 50)
+        var["adjoint_f32dev"] = adjoint_variant(torch, "f32dev")
+        line["variants"] = var
     if not args.no_cpu_baseline:
         # bounded sample of the same workload: estimate one step, then size the run
-        from oracle import oracle as O
         one = cpu_reference_run(n, args.kind, omega, 1, 1, fields)
         steps = max(1, min(50, int(args.cpu_seconds / max(one["seconds"], 1e-3))))
         r = cpu_reference_run(n, args.kind, omega, steps, 0, fields)
@@ -322,7 +470,6 @@ def main() -> None:
             "value": r["mlups"], "unit": "MLUPS", "cores": r["threads"], "kind": "port",
             "sample": f"{n}x{n} {args.kind.upper()} binary64, {steps} steps (two passes each) of the C "
                       f"restatement, {r['threads']} OpenMP threads on {cpu_model()}"}
-        del O
     print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()

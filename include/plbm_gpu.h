@@ -42,13 +42,24 @@ extern "C" {
 #define PLBM_F16DEV  2  /* h_i = f_i - w_i in binary16 scaled by 2^PLBM_F16_SCALE_LOG2 */
 #define PLBM_F16_SCALE_LOG2 15
 
-/* ---- arithmetic of the PLBM_F64 kernels -------------------------------- */
-#define PLBM_MATH_FMA    0  /* binary64, FMA contraction allowed (default)   */
-#define PLBM_MATH_STRICT 1  /* binary64, no contraction: same operations and */
-                            /* order as the Fortran, bit-identical to it     */
-#define PLBM_MATH_HYBRID 2  /* BGK only: exact integer moments, double-float */
-                            /* nonlinear term, binary64 FMAs for the linear  */
-                            /* part; about 18 FP64 instructions per cell     */
+/* ---- arithmetic of the fused step --------------------------------------
+ * PLBM_F64 storage:
+ *   FMA    binary64, FMA contraction allowed (default)
+ *   STRICT binary64, no contraction: the Fortran's operations in its order,
+ *          bit-identical to it
+ *   HYBRID BGK only: exact integer moments, double-float nonlinear term,
+ *          binary64 FMAs for the linear part (about 18 FP64 instructions per
+ *          cell instead of ~70)
+ * Deviation storage (PLBM_F32DEV / PLBM_F16DEV):
+ *   FMA    binary32 collision (default)
+ *   STRICT binary64 collision on the stored deviations
+ *   HYBRID BGK only: compensated binary32 collision (exact pairwise sums,
+ *          hi+lo pairs for the O(h) linear terms, binary32 nonlinear term)
+ *   DF64   BGK only: double-float collision on the stored deviations */
+#define PLBM_MATH_FMA    0
+#define PLBM_MATH_STRICT 1
+#define PLBM_MATH_HYBRID 2
+#define PLBM_MATH_DF64   3
 
 typedef struct plbm_grid plbm_grid_t;
 

@@ -67,5 +67,76 @@ DF_HD void bgk(df64 (&h)[9], const DfParams& p) {
 #undef PLBM_DF_PAIR
 }
 
+// ---- compensated binary32 BGK for deviation storage --------------------------
+// The result is rounded to binary32 (or binary16) storage, so the collision
+// only needs to be accurate well below the spacing of the stored h, not to
+// 48 bits.  The O(h) linear part of the update -- moments, w (drho +- 3 c.j),
+// (1-omega) h -- is carried as an unnormalised hi+lo pair (lazy double-float:
+// no renormalisation, ~44 bits); the nonlinear term
+// omega w rho (4.5 (c.u)^2 - 1.5 u^2), at most ~1e-3, is plain binary32.
+struct DevParams {
+  df64 omb;        // 1 - omega
+  df64 omw[3];     // omega * w  for w0, ws, wd
+  df64 omw3[3];    // 3 omega * w
+  float omwf[3];   // omega * w rounded, for the nonlinear term
+};
+
+DF_HD df64 add_lazy(df64 a, df64 b) {
+  df64 s = two_sum(a.hi, b.hi);
+  s.lo += a.lo + b.lo;
+  return s;
+}
+DF_HD df64 mul_lazy(df64 a, df64 b) {
+  df64 p = two_prod(a.hi, b.hi);
+  p.lo = fmaf_(a.hi, b.lo, p.lo);
+  p.lo = fmaf_(a.lo, b.hi, p.lo);
+  return p;
+}
+DF_HD df64 mul_lazy_f(df64 a, float b) {
+  df64 p = two_prod(a.hi, b);
+  p.lo = fmaf_(a.lo, b, p.lo);
+  return p;
+}
+
+DF_HD void bgk_dev_comp(float (&h)[9], const DevParams& p) {
+  // exact pairwise sums and differences of the stored values
+  const df64 s13 = two_sum(h[1], h[3]), s24 = two_sum(h[2], h[4]);
+  const df64 s57 = two_sum(h[5], h[7]), s68 = two_sum(h[6], h[8]);
+  const df64 d13 = two_sum(h[1], -h[3]), d24 = two_sum(h[2], -h[4]);
+  const df64 d57 = two_sum(h[5], -h[7]), d86 = two_sum(h[8], -h[6]);
+  const df64 drho = add_lazy(add_lazy(add_lazy(s57, s68), add_lazy(s13, s24)), make(h[0], 0.0f));
+  const df64 jx = add_lazy(add_lazy(d57, d86), d13);
+  const df64 jy = add_lazy(add_lazy(d57, neg(d86)), d24);
+  // nonlinear part in binary32: u = j / (1 + drho)
+  const float dr = drho.hi + drho.lo;
+  const float inv = 1.0f / (1.0f + dr);
+  const float jxf = jx.hi + jx.lo, jyf = jy.hi + jy.lo;
+  const float ux = jxf * inv, uy = jyf * inv;
+  const float rho = 1.0f + dr;
+  const float u2 = 1.5f * (ux * ux + uy * uy);
+  // q = 0: h' = (1-w) h0 + omega w0 drho + omega w0 rho (-1.5 u^2)
+  {
+    const float nl = p.omwf[0] * (rho * -u2);
+    const df64 v = add_lazy(add_lazy(mul_lazy_f(p.omb, h[0]), mul_lazy(p.omw[0], drho)), make(nl, 0.0f));
+    h[0] = v.hi + v.lo;
+  }
+#define PLBM_COMP_PAIR(QP, QM, CUF, CJ, WI)                                              \
+  {                                                                                      \
+    const float cu = (CUF);                                                              \
+    const float nl = p.omwf[WI] * (rho * fmaf_(4.5f * cu, cu, -u2));                     \
+    const df64 a = add_lazy(mul_lazy(p.omw[WI], drho), make(nl, 0.0f));                  \
+    const df64 b = mul_lazy(p.omw3[WI], CJ);                                             \
+    const df64 vp = add_lazy(add_lazy(mul_lazy_f(p.omb, h[QP]), a), b);                  \
+    const df64 vm = add_lazy(add_lazy(mul_lazy_f(p.omb, h[QM]), a), neg(b));             \
+    h[QP] = vp.hi + vp.lo;                                                               \
+    h[QM] = vm.hi + vm.lo;                                                               \
+  }
+  PLBM_COMP_PAIR(1, 3, ux, jx, 1)
+  PLBM_COMP_PAIR(2, 4, uy, jy, 1)
+  PLBM_COMP_PAIR(5, 7, ux + uy, add_lazy(jx, jy), 2)
+  PLBM_COMP_PAIR(8, 6, ux - uy, add_lazy(jx, neg(jy)), 2)
+#undef PLBM_COMP_PAIR
+}
+
 }  // namespace df
 }  // namespace plbm

@@ -273,7 +273,9 @@ extern "C" int plbm_set_collision(plbm_grid_t* g, int kind) {
 
 extern "C" int plbm_set_math(plbm_grid_t* g, int math) {
   if (int r = check_grid(g)) return r;
-  if (math < PLBM_MATH_FMA || math > PLBM_MATH_HYBRID) return fail(PLBM_E_INVALID, "unknown math mode %d", math);
+  if (math < PLBM_MATH_FMA || math > PLBM_MATH_DF64) return fail(PLBM_E_INVALID, "unknown math mode %d", math);
+  if (math == PLBM_MATH_DF64 && g->storage == PLBM_F64)
+    return fail(PLBM_E_UNSUPPORTED, "PLBM_MATH_DF64 applies to deviation storage only");
   g->math = math;
   return PLBM_OK;
 }
@@ -345,7 +347,10 @@ namespace {
 // One fused step from lattice a to lattice b with the handle's settings.
 cudaError_t fused_step(plbm_grid_t* g, const void* a, void* b, const CollParams& p) {
   Sweep s{g->nx, g->ny, g->ld, a, b, g->stream};
-  if (g->storage != PLBM_F64) return step_pull_dev(g->storage, g->kind, s, p);
+  if (g->storage != PLBM_F64) {
+    if (g->math == PLBM_MATH_FMA) return step_pull_dev(g->storage, g->kind, s, p);
+    return step_pull_dev_hi(g->storage, g->math, g->kind, s, p);
+  }
   if (g->kind == PLBM_BGKI && g->ld != g->ny) {
     // The (ny,nx,0:8) dummy of collide_bgk_improved does not coincide with the
     // padded lattice: keep the two reference passes.
@@ -387,8 +392,8 @@ extern "C" int plbm_collide(plbm_grid_t* g) {
 extern "C" int plbm_perform_lbm_step(plbm_grid_t* g, int nsteps) {
   if (int r = check_grid(g)) return r;
   if (nsteps < 0) return fail(PLBM_E_INVALID, "nsteps = %d < 0", nsteps);
-  if (g->math == PLBM_MATH_HYBRID && g->storage == PLBM_F64 && g->kind != PLBM_BGK)
-    return fail(PLBM_E_UNSUPPORTED, "PLBM_MATH_HYBRID is offered for collide_bgk only");
+  if ((g->math == PLBM_MATH_HYBRID || g->math == PLBM_MATH_DF64) && g->kind != PLBM_BGK)
+    return fail(PLBM_E_UNSUPPORTED, "PLBM_MATH_HYBRID / PLBM_MATH_DF64 are offered for collide_bgk only");
   if (int r = use_device(g)) return r;
   const CollParams p = plbm_make_params(g->omega, g->trt_magic);
   for (int i = 0; i < nsteps; i++) {

@@ -2,8 +2,13 @@
 // hybrid.cuh (exact integer moments, double-float nonlinear term, binary64
 // FMAs for the final linear combination).  BGK only.
 //
+// Also the deviation-storage steps whose collision runs in more than binary32:
+// double-float (PLBM_MATH_HYBRID) or binary64 (PLBM_MATH_STRICT) arithmetic on
+// h = f - w, stored back in binary32 / scaled binary16.
+//
 // Compiled with --fmad=false: the double-float error-free transformations
 // need every + - * rounded on its own; the fused operations are explicit.
+#include "coll_df64.cuh"
 #include "hybrid.cuh"
 #include "plbm_launch.h"
 
@@ -13,6 +18,68 @@ namespace plbm {
 __device__ int g_hybrid_range_flag = 0;
 
 namespace {
+
+// Deviation storage, BGK evaluated in double-float on h.
+template <class S>
+__global__ void __launch_bounds__(kBlock) k_step_dev_df(const typename S::elem* __restrict__ src,
+                                                       typename S::elem* __restrict__ dst, int nx, int ny, int ld,
+                                                       int ftiles, df::DfParams p) {
+  const int x = blockIdx.x / ftiles;
+  const int y = (blockIdx.x - x * ftiles) * blockDim.x + threadIdx.x;
+  if (y >= ny) return;
+  df::df64 h[9];
+#pragma unroll
+  for (int q = 0; q < 9; q++) {
+    const int sx = wrap_add(x, -cx_of(q), nx), sy = wrap_add(y, -cy_of(q), ny);
+    h[q] = df::make(S::load(src, YFast::off(sx, sy, q, nx, ny, ld)), 0.0f);
+  }
+  df::bgk(h, p);
+#pragma unroll
+  for (int q = 0; q < 9; q++) S::store(dst, YFast::off(x, y, q, nx, ny, ld), h[q].hi + h[q].lo);
+}
+
+// Deviation storage, BGK with the compensated binary32 operator.
+template <class S>
+__global__ void __launch_bounds__(kBlock) k_step_dev_comp(const typename S::elem* __restrict__ src,
+                                                         typename S::elem* __restrict__ dst, int nx, int ny, int ld,
+                                                         int ftiles, df::DevParams p) {
+  const int x = blockIdx.x / ftiles;
+  const int y = (blockIdx.x - x * ftiles) * blockDim.x + threadIdx.x;
+  if (y >= ny) return;
+  float h[9];
+#pragma unroll
+  for (int q = 0; q < 9; q++) {
+    const int sx = wrap_add(x, -cx_of(q), nx), sy = wrap_add(y, -cy_of(q), ny);
+    h[q] = S::load(src, YFast::off(sx, sy, q, nx, ny, ld));
+  }
+  df::bgk_dev_comp(h, p);
+#pragma unroll
+  for (int q = 0; q < 9; q++) S::store(dst, YFast::off(x, y, q, nx, ny, ld), h[q]);
+}
+
+// Deviation storage, collision evaluated in binary64 on h (any kind but BGKI).
+template <class S, int KIND>
+__global__ void __launch_bounds__(kBlock) k_step_dev_d(const typename S::elem* __restrict__ src,
+                                                      typename S::elem* __restrict__ dst, int nx, int ny, int ld,
+                                                      int ftiles, CollParams p) {
+  const int x = blockIdx.x / ftiles;
+  const int y = (blockIdx.x - x * ftiles) * blockDim.x + threadIdx.x;
+  if (y >= ny) return;
+  double h[9];
+#pragma unroll
+  for (int q = 0; q < 9; q++) {
+    const int sx = wrap_add(x, -cx_of(q), nx), sy = wrap_add(y, -cy_of(q), ny);
+    h[q] = (double)S::load(src, YFast::off(sx, sy, q, nx, ny, ld));
+  }
+  collide_shift<KIND, double>(h, p);
+#pragma unroll
+  for (int q = 0; q < 9; q++) S::store(dst, YFast::off(x, y, q, nx, ny, ld), (float)h[q]);
+}
+
+df::df64 split_const(double d) {
+  const float hi = (float)d;
+  return df::make(hi, (float)(d - (double)hi));
+}
 
 __global__ void __launch_bounds__(kBlock) k_step_hybrid_bgk(const double* __restrict__ src,
                                                            double* __restrict__ dst, int nx, int ny, int ld,
@@ -55,6 +122,75 @@ cudaError_t step_pull_df64(int kind, const Sweep& s, const CollParams& cp) {
   k_step_hybrid_bgk<<<(unsigned)blocks, kBlock, 0, s.stream>>>(static_cast<const double*>(s.src),
                                                                static_cast<double*>(s.dst), s.nx, s.ny, s.ld, ft,
                                                                hybrid_params(cp.omega));
+  return cudaGetLastError();
+}
+
+cudaError_t step_pull_dev_hi(int storage, int math, int kind, const Sweep& s, const CollParams& cp) {
+  const int ft = (s.ny + kBlock - 1) / kBlock;
+  const long long blocks = (long long)ft * s.nx;
+  if (blocks <= 0 || blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+  const unsigned nb = (unsigned)blocks;
+  if (math == 2) {  // compensated binary32
+    if (kind != K_BGK) return cudaErrorNotSupported;
+    df::DevParams p;
+    p.omb = split_const(cp.omegabar);
+    const double w[3] = {W0, WS, WD};
+    for (int i = 0; i < 3; i++) {
+      p.omw[i] = split_const(cp.omega * w[i]);
+      p.omw3[i] = split_const(3.0 * cp.omega * w[i]);
+      p.omwf[i] = (float)(cp.omega * w[i]);
+    }
+    if (storage == ST_F32DEV)
+      k_step_dev_comp<StoreF32Dev><<<nb, kBlock, 0, s.stream>>>(static_cast<const float*>(s.src),
+                                                                static_cast<float*>(s.dst), s.nx, s.ny, s.ld, ft, p);
+    else if (storage == ST_F16DEV)
+      k_step_dev_comp<StoreF16Dev><<<nb, kBlock, 0, s.stream>>>(static_cast<const __half*>(s.src),
+                                                                static_cast<__half*>(s.dst), s.nx, s.ny, s.ld, ft, p);
+    else
+      return cudaErrorInvalidValue;
+    return cudaGetLastError();
+  }
+  if (math == 3) {  // double-float
+    if (kind != K_BGK) return cudaErrorNotSupported;
+    df::DfParams p;
+    p.om = split_const(cp.omega);
+    p.omb = split_const(cp.omegabar);
+    p.w0 = split_const(W0);
+    p.ws = split_const(WS);
+    p.wd = split_const(WD);
+    p.ws3 = split_const(3.0 * WS);
+    p.wd3 = split_const(3.0 * WD);
+    if (storage == ST_F32DEV)
+      k_step_dev_df<StoreF32Dev><<<nb, kBlock, 0, s.stream>>>(static_cast<const float*>(s.src),
+                                                              static_cast<float*>(s.dst), s.nx, s.ny, s.ld, ft, p);
+    else if (storage == ST_F16DEV)
+      k_step_dev_df<StoreF16Dev><<<nb, kBlock, 0, s.stream>>>(static_cast<const __half*>(s.src),
+                                                              static_cast<__half*>(s.dst), s.nx, s.ny, s.ld, ft, p);
+    else
+      return cudaErrorInvalidValue;
+    return cudaGetLastError();
+  }
+#define PLBM_DEVD(S, E)                                                                                      \
+  switch (kind) {                                                                                            \
+    case K_BGK: k_step_dev_d<S, K_BGK><<<nb, kBlock, 0, s.stream>>>(static_cast<const E*>(s.src),            \
+                                                                    static_cast<E*>(s.dst), s.nx, s.ny, s.ld, \
+                                                                    ft, cp); break;                           \
+    case K_TRT: k_step_dev_d<S, K_TRT><<<nb, kBlock, 0, s.stream>>>(static_cast<const E*>(s.src),            \
+                                                                    static_cast<E*>(s.dst), s.nx, s.ny, s.ld, \
+                                                                    ft, cp); break;                           \
+    case K_RR: k_step_dev_d<S, K_RR><<<nb, kBlock, 0, s.stream>>>(static_cast<const E*>(s.src),              \
+                                                                  static_cast<E*>(s.dst), s.nx, s.ny, s.ld,   \
+                                                                  ft, cp); break;                             \
+    default: return cudaErrorNotSupported;                                                                   \
+  }
+  if (storage == ST_F32DEV) {
+    PLBM_DEVD(StoreF32Dev, float)
+  } else if (storage == ST_F16DEV) {
+    PLBM_DEVD(StoreF16Dev, __half)
+  } else {
+    return cudaErrorInvalidValue;
+  }
+#undef PLBM_DEVD
   return cudaGetLastError();
 }
 

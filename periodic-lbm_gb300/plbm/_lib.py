@@ -29,8 +29,8 @@ KINDS = {"bgk": BGK, "trt": TRT, "rr": RR, "bgki": BGKI}
 F64, F32DEV, F16DEV = 0, 1, 2
 STORAGES = {"f64": F64, "f32dev": F32DEV, "f16dev": F16DEV}
 # math
-MATH_FMA, MATH_STRICT, MATH_HYBRID = 0, 1, 2
-MATHS = {"fma": MATH_FMA, "strict": MATH_STRICT, "hybrid": MATH_HYBRID}
+MATH_FMA, MATH_STRICT, MATH_HYBRID, MATH_DF64 = 0, 1, 2, 3
+MATHS = {"fma": MATH_FMA, "strict": MATH_STRICT, "hybrid": MATH_HYBRID, "df64": MATH_DF64}
 
 F16_SCALE_LOG2 = 15
 

@@ -51,6 +51,41 @@ def test_deviation_storage_accuracy(gpu_lib, storage, kind, omega):
     assert np.max(np.abs(r - r64)) < (1e-6 if storage == "f32dev" else 1e-2)
 
 
+def run_math(storage, math_mode, n, steps, omega):
+    from plbm import LatticeGrid, cases
+    rho, ux, uy = cases.shear_layer(n, n, float(n), 0.04, 80.0 * n / 8192.0 * 16, 0.05)
+    g = LatticeGrid(n, n, storage=storage, collision="bgk", math=math_mode)
+    g.set_relaxation(omega, 0.25)
+    g.set_pdf_to_equilibrium(rho, ux, uy)
+    g.perform_lbm_step(steps)
+    out = g.update_macros()
+    g.close()
+    return out
+
+
+@pytest.mark.parametrize("storage,math_mode,bound", [("f32dev", "fma", 1e-4), ("f32dev", "hybrid", 2e-6),
+                                                     ("f32dev", "df64", 1e-6), ("f32dev", "strict", 1e-6),
+                                                     ("f16dev", "hybrid", 2e-2)])
+def test_deviation_collision_arithmetic(gpu_lib, storage, math_mode, bound):
+    """Shear layer (BGK, tau = 0.52): binary32 storage with a compensated,
+    double-float or binary64 collision stays within a few binary32 spacings of
+    the binary64 run; the plain binary32 collision drifts much further."""
+    n, steps, omega = 256, 600, 1.0 / 0.52
+    _, u64, v64 = run_math("f64", "hybrid", n, steps, omega)
+    _, u, v = run_math(storage, math_mode, n, steps, omega)
+    err = l2(u, v, u64, v64)
+    print(f"{storage}/{math_mode}: velocity L2 vs binary64 = {err:.3e}")
+    assert err < bound
+
+
+def test_compensated_beats_plain_binary32(gpu_lib):
+    n, steps, omega = 256, 600, 1.0 / 0.52
+    _, u64, v64 = run_math("f64", "hybrid", n, steps, omega)
+    _, ua, va = run_math("f32dev", "fma", n, steps, omega)
+    _, ub, vb = run_math("f32dev", "hybrid", n, steps, omega)
+    assert l2(ub, vb, u64, v64) < 0.2 * l2(ua, va, u64, v64)
+
+
 @pytest.mark.parametrize("storage,tol", [("f32dev", 2e-8), ("f16dev", 2e-5)])
 def test_upload_download_round_trip(gpu_lib, storage, tol):
     from plbm import LatticeGrid
