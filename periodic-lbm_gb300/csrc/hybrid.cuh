@@ -145,5 +145,98 @@ DF_HD void bgk(double (&f)[9], const Params& p, bool& bad) {
 #undef PLBM_HY_PAIR
 }
 
+// ---- fast paths for the ranges lattice states live in --------------------
+// The general conversions are called out of line from the fast paths, so that
+// the compiler branches around them instead of predicating them in.
+#ifdef __CUDACC__
+#define PLBM_NOINLINE __host__ __device__ __noinline__
+#else
+#define PLBM_NOINLINE __attribute__((noinline))
+#endif
+PLBM_NOINLINE int64_t to_fixed_slow(double d, int* bad) {
+  bool b = false;
+  const int64_t r = to_fixed(d, b);
+  if (b) *bad = 1;
+  return r;
+}
+PLBM_NOINLINE double fixed_to_double_slow(int64_t T) { return fixed_to_double(T); }
+
+// High word of (hi:lo) << sh, 0 <= sh <= 31.
+DF_HD uint32_t funnel_l(uint32_t lo, uint32_t hi, uint32_t sh) {
+#ifdef __CUDA_ARCH__
+  return __funnelshift_l(lo, hi, sh);
+#else
+  return sh ? (hi << sh) | (lo >> (32 - sh)) : hi;
+#endif
+}
+
+// to_fixed for positive f in [2^-7, 2): one 64-bit shift by 0..7, the same
+// exact value as the general conversion (which handles everything else).
+DF_HD int64_t to_fixed_fast(double d, bool& bad) {
+  const uint64_t u = df::d2u(d);
+  const uint32_t H = (uint32_t)(u >> 32), L = (uint32_t)u;
+  const uint32_t sh = (H >> 20) - 1016u;  // a set sign bit makes this large
+  if (sh <= 7u) {
+    const uint32_t mh = (H & 0xFFFFFu) | 0x100000u;
+    return (int64_t)(((uint64_t)funnel_l(L, mh, sh) << 32) | (uint64_t)(L << sh));
+  }
+  int b = 0;
+  const int64_t r = to_fixed_slow(d, &b);
+  if (b) bad = true;
+  return r;
+}
+
+// fixed_to_double for 2^58 <= T < 2^60 (values in [0.5, 2)): a shift by 6 or
+// 7 with round-half-up.  It differs from round-to-nearest-even only on exact
+// ties, a few in a thousand values, by one ulp upward (a bias of order 1e-19
+// relative, far below the rounding of the stored state).
+DF_HD double fixed_to_double_fast(int64_t T) {
+  const uint64_t a = (uint64_t)T;
+  const uint32_t top = (uint32_t)(a >> 58);
+  if (top - 1u <= 2u) {
+    const bool big = top >= 2u;
+    const uint32_t sh = big ? 7u : 6u;
+    uint64_t m = (a + (1ull << (sh - 1u))) >> sh;
+    // m <= 2^53; m == 2^53 carries into the exponent through the add below
+    const uint64_t ex = big ? 1023ull : 1022ull;
+    return df::u2d((ex << 52) + (m - (1ull << 52)));
+  }
+  return fixed_to_double_slow(T);
+}
+
+// BGK of the hybrid arithmetic with the fast conversions: the same update as
+// bgk() (rho for the nonlinear term taken from the rounded binary64 R).
+DF_HD void bgk_fast(double (&f)[9], const Params& p, bool& bad) {
+  int64_t F[9];
+#pragma unroll
+  for (int q = 0; q < 9; q++) F[q] = to_fixed_fast(f[q], bad);
+  const int64_t R = (((F[5] + F[7]) + (F[6] + F[8])) + ((F[1] + F[3]) + (F[2] + F[4]))) + F[0];
+  const int64_t d57 = F[5] - F[7], d86 = F[8] - F[6];
+  const int64_t JX = (d57 + d86) + (F[1] - F[3]);
+  const int64_t JY = (d57 - d86) + (F[2] - F[4]);
+  const double Rd = fixed_to_double_fast(R);
+  const df64 rho = df::from_double(Rd);
+  const df64 inv = df::recip(rho);
+  const df64 ux = df::mul(fixed_to_df(JX), inv), uy = df::mul(fixed_to_df(JY), inv);
+  const df64 u2_15 = df::mul_f(df::add(df::sqr(ux), df::sqr(uy)), 1.5f);
+  {
+    const double c0 = df::pack_double(df::neg(df::mul(p.omw_df[0], df::mul(rho, u2_15))));
+    f[0] = fma_d(p.omw[0], Rd, fma_d(p.omb, f[0], c0));
+  }
+#define PLBM_HY_PAIR(QP, QM, CU, CJ, WI)                                                    \
+  {                                                                                         \
+    const double c = df::pack_double(                                                       \
+        df::mul(p.omw_df[WI], df::mul(rho, df::sub(df::mul_f(df::sqr(CU), 4.5f), u2_15))));  \
+    const int64_t cj3 = (CJ) + ((CJ) << 1);                                                 \
+    f[QP] = fma_d(p.omw[WI], fixed_to_double_fast(R + cj3), fma_d(p.omb, f[QP], c));        \
+    f[QM] = fma_d(p.omw[WI], fixed_to_double_fast(R - cj3), fma_d(p.omb, f[QM], c));        \
+  }
+  PLBM_HY_PAIR(1, 3, ux, JX, 1)
+  PLBM_HY_PAIR(2, 4, uy, JY, 1)
+  PLBM_HY_PAIR(5, 7, df::add(ux, uy), JX + JY, 2)
+  PLBM_HY_PAIR(8, 6, df::sub(ux, uy), JX - JY, 2)
+#undef PLBM_HY_PAIR
+}
+
 }  // namespace hy
 }  // namespace plbm

@@ -81,23 +81,36 @@ df::df64 split_const(double d) {
   return df::make(hi, (float)(d - (double)hi));
 }
 
+// I: index type of the lattice offsets; 32-bit when the whole lattice has
+// fewer than 2^32 elements (one multiply-add per address instead of 64-bit
+// arithmetic).
+template <typename I>
 __global__ void __launch_bounds__(kBlock) k_step_hybrid_bgk(const double* __restrict__ src,
                                                            double* __restrict__ dst, int nx, int ny, int ld,
                                                            int ftiles, hy::Params p) {
   const int x = blockIdx.x / ftiles;
   const int y = (blockIdx.x - x * ftiles) * blockDim.x + threadIdx.x;
   if (y >= ny) return;
+  const I L = (I)ld, P = (I)ld * (I)nx;
+  const I c0 = (I)x * L, cm = (I)wrap_m(x, nx) * L, cp = (I)wrap_p(x, nx) * L;
+  const I y0 = (I)y, ym = (I)wrap_m(y, ny), yp = (I)wrap_p(y, ny);
   double f[9];
-#pragma unroll
-  for (int q = 0; q < 9; q++) {
-    const int sx = wrap_add(x, -cx_of(q), nx), sy = wrap_add(y, -cy_of(q), ny);
-    f[q] = __ldg(src + YFast::off(sx, sy, q, nx, ny, ld));
-  }
+  // pull: f_q(x, y) = f_q(x - cx_q, y - cy_q) of the source lattice
+  f[0] = __ldg(src + (c0 + y0));
+  f[1] = __ldg(src + (P + cm + y0));
+  f[2] = __ldg(src + (2 * P + c0 + ym));
+  f[3] = __ldg(src + (3 * P + cp + y0));
+  f[4] = __ldg(src + (4 * P + c0 + yp));
+  f[5] = __ldg(src + (5 * P + cm + ym));
+  f[6] = __ldg(src + (6 * P + cp + ym));
+  f[7] = __ldg(src + (7 * P + cp + yp));
+  f[8] = __ldg(src + (8 * P + cm + yp));
   bool bad = false;
-  hy::bgk(f, p, bad);
+  hy::bgk_fast(f, p, bad);
   if (bad) g_hybrid_range_flag = 1;
+  const I o = c0 + y0;
 #pragma unroll
-  for (int q = 0; q < 9; q++) dst[YFast::off(x, y, q, nx, ny, ld)] = f[q];
+  for (int q = 0; q < 9; q++) dst[(I)q * P + o] = f[q];
 }
 
 }  // namespace
@@ -119,9 +132,14 @@ cudaError_t step_pull_df64(int kind, const Sweep& s, const CollParams& cp) {
   const int ft = (s.ny + kBlock - 1) / kBlock;
   const long long blocks = (long long)ft * s.nx;
   if (blocks <= 0 || blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
-  k_step_hybrid_bgk<<<(unsigned)blocks, kBlock, 0, s.stream>>>(static_cast<const double*>(s.src),
-                                                               static_cast<double*>(s.dst), s.nx, s.ny, s.ld, ft,
-                                                               hybrid_params(cp.omega));
+  const double* a = static_cast<const double*>(s.src);
+  double* b = static_cast<double*>(s.dst);
+  if ((unsigned long long)s.ld * (unsigned long long)s.nx * 9ull < (1ull << 32))
+    k_step_hybrid_bgk<uint32_t><<<(unsigned)blocks, kBlock, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft,
+                                                                           hybrid_params(cp.omega));
+  else
+    k_step_hybrid_bgk<size_t><<<(unsigned)blocks, kBlock, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft,
+                                                                         hybrid_params(cp.omega));
   return cudaGetLastError();
 }
 
