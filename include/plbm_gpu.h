@@ -205,6 +205,11 @@ int plbm_batch_info(const plbm_batch_t *b, int *ngrids, long long *cells, int *n
 int plbm_batch_set_schedule(plbm_batch_t *b, const plbm_batch_schedule *s);
 int plbm_batch_get_schedule(const plbm_batch_t *b, plbm_batch_schedule *s);
 int plbm_batch_set_stream(plbm_batch_t *b, void *cuda_stream);
+/* Collision arithmetic of the batch: PLBM_MATH_FMA (default) for every
+ * storage, or PLBM_MATH_HYBRID for PLBM_F64 (its BGK grids take the hybrid
+ * binary64 arithmetic of plbm_set_math; a cell with some |f_q| >= 2 falls
+ * back to the FMA BGK; TRT grids stay FMA). */
+int plbm_batch_set_math(plbm_batch_t *b, int math);
 /* Equilibrium of host (ny,nx) rho/ux/uy into the current lattice of grid i
  * (set_pdf_to_equilibrium, src/fvm_bardow.F90:272-305). */
 int plbm_batch_set_equilibrium(plbm_batch_t *b, int grid, const double *rho, const double *ux,

@@ -25,10 +25,13 @@ CollParams plbm_make_params(double omega, double trt_magic);
   } while (0)
 
 struct plbm_batch {
-  int ngrids = 0, storage = 0, device = 0, sms = 0;
+  int ngrids = 0, storage = 0, device = 0, sms = 0, math = PLBM_MATH_FMA;
   std::vector<BatchGrid> grids;   // host copy (off, sizes, params, ty)
   BatchGrid* d_grids = nullptr;
   int* d_tile_start = nullptr;
+  int* d_tile_grid = nullptr;   // grid index of each tile (capacity tile_cap)
+  size_t tile_cap = 0;
+  int small_index = 1;          // every lattice pair has < 2^32 elements
   int ntiles = 0;
   long long cells = 0;
   size_t elems = 0, elem_bytes = 8;
@@ -85,12 +88,24 @@ int apply_schedule(plbm_batch_t* b) {
     start[i + 1] = start[i] + (int)t;
   }
   b->ntiles = start[b->ngrids];
+  std::vector<int> owner((size_t)b->ntiles);
+  for (int i = 0; i < b->ngrids; i++)
+    for (int t = start[i]; t < start[i + 1]; t++) owner[(size_t)t] = i;
+  if ((size_t)b->ntiles > b->tile_cap) {
+    if (b->d_tile_grid) cudaFree(b->d_tile_grid);
+    b->d_tile_grid = nullptr;
+    b->tile_cap = 0;
+    CUDA_TRY(cudaMalloc(&b->d_tile_grid, sizeof(int) * (size_t)b->ntiles), "cudaMalloc(tile table)");
+    b->tile_cap = (size_t)b->ntiles;
+  }
   CUDA_TRY(cudaMemcpy(b->d_grids, b->grids.data(), sizeof(BatchGrid) * b->ngrids, cudaMemcpyHostToDevice),
            "upload batch table");
   CUDA_TRY(cudaMemcpy(b->d_tile_start, start.data(), sizeof(int) * (b->ngrids + 1), cudaMemcpyHostToDevice),
            "upload tile table");
+  CUDA_TRY(cudaMemcpy(b->d_tile_grid, owner.data(), sizeof(int) * owner.size(), cudaMemcpyHostToDevice),
+           "upload tile owners");
   int per_sm = 0;
-  CUDA_TRY(batch_max_ctas(b->storage, b->sched.threads, &per_sm), "occupancy");
+  CUDA_TRY(batch_max_ctas(b->storage, b->sched.threads, b->small_index, &per_sm), "occupancy");
   if (per_sm < 1) return fail(PLBM_E_UNSUPPORTED, "batched kernel does not fit on an SM with %d threads", b->sched.threads);
   const int want = b->sched.ctas_per_sm > 0 ? std::min(b->sched.ctas_per_sm, per_sm) : per_sm;
   b->ctas = std::max(1, std::min(b->ntiles, want * b->sms));
@@ -102,6 +117,8 @@ BatchLaunch launch_of(const plbm_batch_t* b) {
   BatchLaunch L;
   L.grids = b->d_grids;
   L.tile_start = b->d_tile_start;
+  L.tile_grid = b->d_tile_grid;
+  L.small_index = b->small_index;
   L.ngrids = b->ngrids;
   L.ntiles = b->ntiles;
   L.threads = b->sched.threads;
@@ -185,8 +202,10 @@ extern "C" int plbm_batch_create(int ngrids, const int* nx, const int* ny, const
     g.ld = pad16(ny[i]);
     g.kind = kind[i];
     g.p = plbm_make_params(omega[i], trt_magic ? trt_magic[i] : 0.25);
+    g.hp = hybrid_params(omega[i]);
     g.off = (long long)off;
     off += 2 * (size_t)g.ld * g.nx * 9;
+    if (2 * (unsigned long long)g.ld * g.nx * 9 >= (1ull << 32)) b->small_index = 0;
     b->cells += (long long)g.nx * g.ny;
   }
   b->elems = off;
@@ -219,6 +238,7 @@ extern "C" int plbm_batch_destroy(plbm_batch_t* b) {
   cudaFree(b->base);
   cudaFree(b->d_grids);
   cudaFree(b->d_tile_start);
+  cudaFree(b->d_tile_grid);
   cudaFree(b->ctrl);
   cudaFree(b->scratch);
   if (b->own) cudaStreamDestroy(b->own);
@@ -255,6 +275,19 @@ extern "C" int plbm_batch_set_stream(plbm_batch_t* b, void* stream) {
   b->stream = stream ? static_cast<cudaStream_t>(stream) : b->own;
   drop_graphs(b);
   return PLBM_OK;
+}
+
+extern "C" int plbm_batch_set_math(plbm_batch_t* b, int math) {
+  if (!b) return fail(PLBM_E_INVALID, "NULL batch");
+  if (math != PLBM_MATH_FMA && math != PLBM_MATH_HYBRID)
+    return fail(PLBM_E_UNSUPPORTED, "batched math %d (PLBM_MATH_FMA or PLBM_MATH_HYBRID)", math);
+  if (math == PLBM_MATH_HYBRID && b->storage != PLBM_F64)
+    return fail(PLBM_E_UNSUPPORTED, "PLBM_MATH_HYBRID needs PLBM_F64 storage");
+  CUDA_TRY(cudaSetDevice(b->device), "cudaSetDevice");
+  CUDA_TRY(cudaStreamSynchronize(b->stream), "synchronize");
+  for (BatchGrid& g : b->grids) g.hybrid = (math == PLBM_MATH_HYBRID && g.kind == PLBM_BGK) ? 1 : 0;
+  b->math = math;
+  return apply_schedule(b);
 }
 
 extern "C" int plbm_batch_set_equilibrium(plbm_batch_t* b, int grid, const double* rho, const double* ux,

@@ -37,15 +37,17 @@ struct alignas(16) Ctrl {
   int where;          // step at which the timeout happened
 };
 
-template <class S>
-__device__ __forceinline__ typename S::real load_cg(const typename S::elem* p, size_t i);
-template <>
-__device__ __forceinline__ double load_cg<StoreF64>(const double* p, size_t i) { return __ldcg(p + i); }
-template <>
-__device__ __forceinline__ float load_cg<StoreF32Dev>(const float* p, size_t i) { return __ldcg(p + i); }
+// Population load: ld.global.cg (L2 only) inside the persistent kernel, the
+// read-only path in the per-step kernel.
+template <bool CG, typename E>
+__device__ __forceinline__ E load_pop(const E* p) {
+  if constexpr (CG) return __ldcg(p);
+  else return __ldg(p);
+}
 
-// Process one tile of one grid for one step.
-template <class S>
+// Process one tile of one grid for one step.  I: index type inside one grid's
+// lattice pair (32-bit when every grid's pair has fewer than 2^32 elements).
+template <class S, bool CG, typename I>
 __device__ __forceinline__ void do_tile(const BatchGrid& g, int local_tile, int parity,
                                         typename S::elem* __restrict__ base) {
   const int ty = g.ty;
@@ -55,51 +57,61 @@ __device__ __forceinline__ void do_tile(const BatchGrid& g, int local_tile, int 
   const int y = tyi * ty + (int)(threadIdx.x % ty);
   const int x = txi * tx + (int)(threadIdx.x / ty);
   if (x >= g.nx || y >= g.ny) return;
-  const size_t lat = (size_t)g.ld * g.nx * 9;
+  const I L = (I)g.ld, P = (I)g.ld * (I)g.nx, lat = 9 * P;
   const typename S::elem* src = base + g.off + (parity ? lat : 0);
   typename S::elem* dst = base + g.off + (parity ? 0 : lat);
+  const I c0 = (I)x * L, cm = (I)wrap_m(x, g.nx) * L, cp = (I)wrap_p(x, g.nx) * L;
+  const I y0 = (I)y, ym = (I)wrap_m(y, g.ny), yp = (I)wrap_p(y, g.ny);
+  typedef typename S::elem E;
+  E e[9];
+  e[0] = load_pop<CG>(src + (c0 + y0));
+  e[1] = load_pop<CG>(src + (P + cm + y0));
+  e[2] = load_pop<CG>(src + (2 * P + c0 + ym));
+  e[3] = load_pop<CG>(src + (3 * P + cp + y0));
+  e[4] = load_pop<CG>(src + (4 * P + c0 + yp));
+  e[5] = load_pop<CG>(src + (5 * P + cm + ym));
+  e[6] = load_pop<CG>(src + (6 * P + cp + ym));
+  e[7] = load_pop<CG>(src + (7 * P + cp + yp));
+  e[8] = load_pop<CG>(src + (8 * P + cm + yp));
   typename S::real f[9];
 #pragma unroll
-  for (int q = 0; q < 9; q++) {
-    const int sx = wrap_add(x, -cx_of(q), g.nx), sy = wrap_add(y, -cy_of(q), g.ny);
-    f[q] = load_cg<S>(src, YFast::off(sx, sy, q, g.nx, g.ny, g.ld));
-  }
+  for (int q = 0; q < 9; q++) f[q] = (typename S::real)e[q];
   if constexpr (S::ddf) {
     if (g.kind == K_TRT) collide_shift<K_TRT, typename S::real>(f, g.p);
     else collide_shift<K_BGK, typename S::real>(f, g.p);
   } else {
-    if (g.kind == K_TRT) collide_ref<K_TRT>(f, g.p);
-    else collide_ref<K_BGK>(f, g.p);
-  }
+    if (g.kind == K_TRT) {
+      collide_ref<K_TRT>(f, g.p);
+    } else if (g.hybrid) {
+      double keep[9];
 #pragma unroll
-  for (int q = 0; q < 9; q++) S::store(dst, YFast::off(x, y, q, g.nx, g.ny, g.ld), f[q]);
-}
-
-__device__ __forceinline__ int find_grid(const int* __restrict__ tile_start, int ngrids, int t) {
-  // largest g with tile_start[g] <= t
-  int lo = 0, hi = ngrids - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (__ldg(tile_start + mid) <= t) lo = mid;
-    else hi = mid - 1;
-  }
-  return lo;
-}
-
-template <class S>
-__device__ __forceinline__ void sweep(const BatchGrid* __restrict__ grids, const int* __restrict__ tile_start,
-                                      int ngrids, int ntiles, int parity, typename S::elem* base) {
-  __shared__ BatchGrid sg;
-  __shared__ int sgi;
-  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      const int gi = find_grid(tile_start, ngrids, t);
-      sgi = gi;
-      sg = grids[gi];
+      for (int q = 0; q < 9; q++) keep[q] = f[q];
+      bool bad = false;
+      hy::bgk_fast(f, g.hp, bad);
+      if (bad) {  // outside the hybrid range (|f| >= 2): straight binary64 BGK
+#pragma unroll
+        for (int q = 0; q < 9; q++) f[q] = keep[q];
+        collide_ref<K_BGK>(f, g.p);
+      }
+    } else {
+      collide_ref<K_BGK>(f, g.p);
     }
-    __syncthreads();
-    do_tile<S>(sg, t - __ldg(tile_start + sgi), parity, base);
+  }
+  const I o = c0 + y0;
+#pragma unroll
+  for (int q = 0; q < 9; q++) S::store(dst, (size_t)((I)q * P + o), f[q]);
+}
+
+// Tiles t = blockIdx.x, blockIdx.x + gridDim.x, ...; the grid of tile t is
+// tile_grid[t] (precomputed), its first tile tile_start[grid].
+template <class S, bool CG, typename I>
+__device__ __forceinline__ void sweep(const BatchGrid* __restrict__ grids, const int* __restrict__ tile_start,
+                                      const int* __restrict__ tile_grid, int ntiles, int parity,
+                                      typename S::elem* base) {
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int gi = __ldg(tile_grid + t);
+    const BatchGrid g = grids[gi];
+    do_tile<S, CG, I>(g, t - __ldg(tile_start + gi), parity, base);
   }
 }
 
@@ -136,26 +148,27 @@ __device__ __forceinline__ bool barrier(Ctrl* ctrl, int step) {
   return ok != 0;
 }
 
-template <class S>
+template <class S, typename I>
 __global__ void __launch_bounds__(kBatchMaxThreads) k_batch_persistent(const BatchGrid* __restrict__ grids,
                                                                       const int* __restrict__ tile_start,
-                                                                      int ngrids, int ntiles, int nsteps,
-                                                                      int parity0, typename S::elem* base,
-                                                                      Ctrl* ctrl) {
+                                                                      const int* __restrict__ tile_grid,
+                                                                      int ntiles, int nsteps, int parity0,
+                                                                      typename S::elem* base, Ctrl* ctrl) {
   for (int s = 0; s < nsteps; s++) {
-    sweep<S>(grids, tile_start, ngrids, ntiles, (parity0 + s) & 1, base);
+    sweep<S, true, I>(grids, tile_start, tile_grid, ntiles, (parity0 + s) & 1, base);
     if (s + 1 < nsteps && !barrier(ctrl, s)) return;
   }
 }
 
-template <class S>
+template <class S, typename I>
 __global__ void __launch_bounds__(kBatchMaxThreads) k_batch_step(const BatchGrid* __restrict__ grids,
-                                                                const int* __restrict__ tile_start, int ngrids,
-                                                                int ntiles, int parity, typename S::elem* base) {
-  sweep<S>(grids, tile_start, ngrids, ntiles, parity, base);
+                                                                const int* __restrict__ tile_start,
+                                                                const int* __restrict__ tile_grid, int ntiles,
+                                                                int parity, typename S::elem* base) {
+  sweep<S, false, I>(grids, tile_start, tile_grid, ntiles, parity, base);
 }
 
-template <class S>
+template <class S, typename I>
 cudaError_t launch_batch(const BatchLaunch& L, int nsteps, int parity0) {
   typedef typename S::elem E;
   E* base = static_cast<E*>(L.base);
@@ -170,33 +183,46 @@ cudaError_t launch_batch(const BatchLaunch& L, int nsteps, int parity0) {
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, k_batch_persistent<S>, L.grids, L.tile_start, L.ngrids, L.ntiles, nsteps,
+    return cudaLaunchKernelEx(&cfg, k_batch_persistent<S, I>, L.grids, L.tile_start, L.tile_grid, L.ntiles, nsteps,
                               parity0, base, ctrl);
   }
+  // one tile per CTA
   for (int s = 0; s < nsteps; s++) {
-    k_batch_step<S><<<L.ctas, L.threads, 0, L.stream>>>(L.grids, L.tile_start, L.ngrids, L.ntiles,
-                                                         (parity0 + s) & 1, base);
+    k_batch_step<S, I><<<L.ntiles, L.threads, 0, L.stream>>>(L.grids, L.tile_start, L.tile_grid, L.ntiles,
+                                                             (parity0 + s) & 1, base);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
 }
 
+template <class S>
+cudaError_t launch_batch_i(const BatchLaunch& L, int nsteps, int parity0) {
+  if (L.small_index) return launch_batch<S, uint32_t>(L, nsteps, parity0);
+  return launch_batch<S, size_t>(L, nsteps, parity0);
+}
+
 }  // namespace
 
 size_t batch_ctrl_bytes() { return sizeof(Ctrl); }
 
-cudaError_t batch_max_ctas(int storage, int threads, int* per_sm) {
+cudaError_t batch_max_ctas(int storage, int threads, int small_index, int* per_sm) {
   if (storage == ST_F64)
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_batch_persistent<StoreF64>, threads, 0);
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_batch_persistent<StoreF32Dev>, threads, 0);
+    return small_index ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_batch_persistent<StoreF64, uint32_t>,
+                                                                     threads, 0)
+                       : cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_batch_persistent<StoreF64, size_t>,
+                                                                     threads, 0);
+  return small_index ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_batch_persistent<StoreF32Dev, uint32_t>,
+                                                                   threads, 0)
+                     : cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_batch_persistent<StoreF32Dev, size_t>,
+                                                                   threads, 0);
 }
 
 cudaError_t batch_run(int storage, const BatchLaunch& L, int nsteps, int parity0) {
   if (nsteps <= 0) return cudaSuccess;
   if (L.threads <= 0 || L.threads > kBatchMaxThreads || (L.threads & 31)) return cudaErrorInvalidConfiguration;
-  if (storage == ST_F64) return launch_batch<StoreF64>(L, nsteps, parity0);
-  if (storage == ST_F32DEV) return launch_batch<StoreF32Dev>(L, nsteps, parity0);
+  if (storage == ST_F64) return launch_batch_i<StoreF64>(L, nsteps, parity0);
+  if (storage == ST_F32DEV) return launch_batch_i<StoreF32Dev>(L, nsteps, parity0);
   return cudaErrorNotSupported;
 }
 

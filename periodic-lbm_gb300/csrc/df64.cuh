@@ -15,10 +15,11 @@
 // F2F conversions between binary32 and binary64 run at the binary64 rate.
 //
 // Every function is __host__ __device__ so the same code can be checked on
-// the CPU.  Translation units using this header must be compiled without FMA
-// contraction (--fmad=false / -ffp-contract=off): the error-free
-// transformations assume each + - * is rounded separately, and the only
-// fused operations are the explicit fmaf calls.
+// the CPU.  The error-free transformations assume each + - * is rounded
+// separately and the only fused operations are the explicit fmaf calls; the
+// one product that feeds an add (two_prod) uses an explicitly rounded
+// multiply, so contraction settings of the including translation unit cannot
+// fuse it (host code is compiled with -ffp-contract=off).
 #pragma once
 #include <stdint.h>
 #include <string.h>
@@ -108,8 +109,19 @@ DF_HD df64 fast_two_sum(float a, float b) {
   return make(s, e);
 }
 
+// Product rounded on its own: never fused into a following add, whatever the
+// translation unit's contraction setting (the error-free transformations need
+// p = RN(a*b) exactly).
+DF_HD float mul_rn(float a, float b) {
+#ifdef __CUDA_ARCH__
+  return __fmul_rn(a, b);
+#else
+  return a * b;
+#endif
+}
+
 DF_HD df64 two_prod(float a, float b) {
-  float p = a * b;
+  float p = mul_rn(a, b);
   float e = fmaf_(a, b, -p);
   return make(p, e);
 }

@@ -149,9 +149,9 @@ DF_HD void bgk(double (&f)[9], const Params& p, bool& bad) {
 // The general conversions are called out of line from the fast paths, so that
 // the compiler branches around them instead of predicating them in.
 #ifdef __CUDACC__
-#define PLBM_NOINLINE __host__ __device__ __noinline__
+#define PLBM_NOINLINE static __host__ __device__ __noinline__
 #else
-#define PLBM_NOINLINE __attribute__((noinline))
+#define PLBM_NOINLINE static __attribute__((noinline))
 #endif
 PLBM_NOINLINE int64_t to_fixed_slow(double d, int* bad) {
   bool b = false;

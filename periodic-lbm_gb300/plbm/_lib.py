@@ -97,6 +97,7 @@ SIGNATURES = {
     "plbm_batch_set_schedule": (C.c_int, [_vp, _vp]),
     "plbm_batch_get_schedule": (C.c_int, [_vp, _vp]),
     "plbm_batch_set_stream": (C.c_int, [_vp, _vp]),
+    "plbm_batch_set_math": (C.c_int, [_vp, C.c_int]),
     "plbm_batch_set_equilibrium": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp]),
     "plbm_batch_run": (C.c_int, [_vp, C.c_int]),
     "plbm_batch_capture": (C.c_int, [_vp, C.c_int]),

@@ -11,7 +11,7 @@ runs of the actual batch with CUDA events:
 3. resident CTAs per SM in {occupancy maximum, 1, 2, 4}.
 
 The winner is cached in a JSON file keyed by the batch signature (grid sizes,
-kinds, storage, device), so later runs of the same batch reuse it.  The
+kinds, storage, collision arithmetic, device), so later runs of the same batch reuse it.  The
 schedule changes only the work decomposition: results are bit-identical for
 every schedule.
 """
@@ -39,7 +39,7 @@ def signature(batch: BatchedGrids, device: str) -> str:
     h = hashlib.sha256()
     for s in batch.specs:
         h.update(f"{s.nx},{s.ny},{s.kind};".encode())
-    h.update(f"{batch.storage}|{device}".encode())
+    h.update(f"{batch.storage}|{getattr(batch, 'math', 'fma')}|{device}".encode())
     return h.hexdigest()[:24]
 
 

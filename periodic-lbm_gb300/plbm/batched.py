@@ -60,7 +60,7 @@ class GridSpec:
 class BatchedGrids:
     """A device batch of periodic grids; state lives on the GPU."""
 
-    def __init__(self, specs: list[GridSpec], storage: str = "f64"):
+    def __init__(self, specs: list[GridSpec], storage: str = "f64", math: str = "fma"):
         self._lib = _bind()
         self.specs = list(specs)
         n = len(specs)
@@ -74,6 +74,14 @@ class BatchedGrids:
                                           _lib.STORAGES[storage], C.byref(h)))
         self._h = h
         self.storage = storage
+        self.math = "fma"
+        if math != "fma":
+            self.set_math(math)
+
+    def set_math(self, math: str) -> None:
+        """"fma" or, for binary64 storage, "hybrid" (BGK grids only)."""
+        check(self._lib.plbm_batch_set_math(self._h, _lib.MATHS[math]))
+        self.math = math
 
     def close(self):
         if getattr(self, "_h", None) is not None and self._h.value:

@@ -141,3 +141,58 @@ def test_batch_input_errors(gpu_lib):
     with pytest.raises(PlbmError):
         b.launch_graph()  # nothing captured
     b.close()
+
+
+def make_batch_math(storage, math):
+    b, fields = make_batch(storage)
+    b.set_math(math)
+    return b, fields
+
+
+def test_batched_hybrid_matches_oracle_per_grid(gpu_lib):
+    """Hybrid binary64 arithmetic on the BGK grids (TRT grids stay FMA):
+    every grid within 1e-12 of the oracle, and independent of the schedule."""
+    from plbm.batched import Schedule
+    b, fields = make_batch_math("f64", "hybrid")
+    b.run(7)
+    b.run(6)
+    for i, (nx, ny, _, _) in enumerate(SPECS):
+        got = b.download(i)
+        ref = oracle_grid(i, fields, 13)
+        for a, c in zip(O.update_macros(got, ny), O.update_macros(ref, ny)):
+            assert relinf(a, c) <= 1e-12
+    want = _states(b)
+    b.close()
+    p, _ = make_batch_math("f64", "hybrid")
+    p.schedule = Schedule.from_dict({"threads": 128, "ctas_per_sm": 0, "persistent": 0, "ty": [32] * 5})
+    p.run(13)
+    for x, y in zip(_states(p), want):
+        assert np.array_equal(x, y)
+    p.close()
+
+
+def test_batched_hybrid_falls_back_outside_range(gpu_lib):
+    """A BGK grid holding |f| >= 2 takes the FMA BGK in those cells: the
+    result equals the FMA batch's to 1e-12."""
+    from plbm.batched import BatchedGrids, GridSpec
+    specs = [GridSpec(16, 32, "bgk", 1.3)]
+    rng = np.random.default_rng(9)
+    rho = 5.0 + 0.01 * rng.standard_normal((16, 32))  # f_0 = 4/9 rho > 2
+    ux = 0.02 * rng.standard_normal((16, 32))
+    uy = 0.02 * rng.standard_normal((16, 32))
+    outs = []
+    for m in ("fma", "hybrid"):
+        b = BatchedGrids(specs, "f64", math=m)
+        b.set_equilibrium(0, rho, ux, uy)
+        b.run(5)
+        outs.append(b.download(0))
+        b.close()
+    assert relinf(outs[1], outs[0]) <= 1e-12
+
+
+def test_batched_hybrid_rejected_for_f32dev(gpu_lib):
+    from plbm import PlbmError
+    b, _ = make_batch("f32dev")
+    with pytest.raises(PlbmError):
+        b.set_math("hybrid")
+    b.close()
