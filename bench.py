@@ -249,9 +249,10 @@ def mixed_precision_errors(torch, n, tau, checkpoints):
     return out
 
 
-def batched_variant(torch, storage, steps):
+def batched_variant(torch, storage, steps, math="fma"):
     from plbm import autotune, batched
     b = batched.build_tgv_batch(512, 2024, storage)
+    b.set_math(math)
     _, rep = autotune.tune(b, steps=5, reps=1, use_cache=True)
     stream = torch.cuda.Stream()
     b.set_stream(stream.cuda_stream)
@@ -269,7 +270,7 @@ def batched_variant(torch, storage, steps):
     cells = b.cells
     b.close()
     mlups = cells * steps / (ms * 1e-3) / 1e6
-    return {"value": mlups, "unit": "MLUPS", "grids": 512, "cells": cells, "steps_per_graph": steps,
+    return {"value": mlups, "unit": "MLUPS", "grids": 512, "cells": cells, "math": math, "steps_per_graph": steps,
             "ms_per_step": ms / steps, "schedule": rep["schedule"], "schedule_cached": rep.get("cached", False),
             "achieved_gbs": mlups * 1e6 * BYTES_PER_CELL[storage] / 1e9}
 
@@ -457,7 +458,8 @@ def main() -> None:
         var["mixed_precision_l2_vs_f64"] = {
             "workload": f"shear layer {n}^2 BGK tau=0.52 k=80 delta=0.05 u0=0.04, step 1000 "
                         "(steps 5000/20000: bench.py --suite mixed)", **mp}
-        var["batched_f64"] = batched_variant(torch, "f64", 50)
+        var["batched_f64"] = batched_variant(torch, "f64", 50, "hybrid")
+        var["batched_f64_fma"] = batched_variant(torch, "f64", 50)
         var["batched_f32dev"] = batched_variant(torch, "f32dev", 50)
         var["adjoint_f32dev"] = adjoint_variant(torch, "f32dev")
         line["variants"] = var

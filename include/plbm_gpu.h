@@ -47,9 +47,11 @@ extern "C" {
  *   FMA    binary64, FMA contraction allowed (default)
  *   STRICT binary64, no contraction: the Fortran's operations in its order,
  *          bit-identical to it
- *   HYBRID BGK only: exact integer moments, double-float nonlinear term,
- *          binary64 FMAs for the linear part (about 18 FP64 instructions per
- *          cell instead of ~70)
+ *   HYBRID BGK and TRT: exact integer moments, double-float for the small
+ *          terms, binary64 only for the final combination (BGK: 18 FP64
+ *          instructions per cell instead of ~70; TRT: 10).  A cell with
+ *          |f_0| >= 2, |f_axis| >= 1/2 or |f_diagonal| >= 1/4 is evaluated
+ *          with the FMA binary64 operator instead (see plbm_hybrid_range_flag)
  * Deviation storage (PLBM_F32DEV / PLBM_F16DEV):
  *   FMA    binary32 collision (default)
  *   STRICT binary64 collision on the stored deviations
@@ -164,10 +166,12 @@ int plbm_velocity_l2_error_noalloc(int storage, int nx, int ny, int ld, const vo
 /* Wait for all work queued on the handle's stream. */
 int plbm_synchronize(plbm_grid_t *g);
 
-/* PLBM_MATH_HYBRID needs |f_q| < 2 for every population; a kernel that met
- * one outside sets a device flag.  Reads it (after synchronising the device)
- * and clears it when reset != 0.  No reference counterpart (the reference has
- * no such mode). */
+/* PLBM_MATH_HYBRID with PLBM_F64 storage evaluates a cell outside its range
+ * (|f_0| >= 2, |f_axis| >= 1/2 or |f_diagonal| >= 1/4) with the binary64
+ * operator and sets a device flag: results stay valid, the flag only reports
+ * that the slower path ran.  Reads it (after synchronising the device) and
+ * clears it when reset != 0.  No reference counterpart (the reference has no
+ * such mode). */
 int plbm_hybrid_range_flag(int *flag, int reset);
 
 /* ---- batched grids ------------------------------------------------------
@@ -206,9 +210,9 @@ int plbm_batch_set_schedule(plbm_batch_t *b, const plbm_batch_schedule *s);
 int plbm_batch_get_schedule(const plbm_batch_t *b, plbm_batch_schedule *s);
 int plbm_batch_set_stream(plbm_batch_t *b, void *cuda_stream);
 /* Collision arithmetic of the batch: PLBM_MATH_FMA (default) for every
- * storage, or PLBM_MATH_HYBRID for PLBM_F64 (its BGK grids take the hybrid
- * binary64 arithmetic of plbm_set_math; a cell with some |f_q| >= 2 falls
- * back to the FMA BGK; TRT grids stay FMA). */
+ * storage, or PLBM_MATH_HYBRID for PLBM_F64 (BGK and TRT grids alike take
+ * the hybrid binary64 arithmetic of plbm_set_math; a cell outside its range
+ * takes the FMA binary64 operator). */
 int plbm_batch_set_math(plbm_batch_t *b, int math);
 /* Equilibrium of host (ny,nx) rho/ux/uy into the current lattice of grid i
  * (set_pdf_to_equilibrium, src/fvm_bardow.F90:272-305). */

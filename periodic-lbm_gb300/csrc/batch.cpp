@@ -203,6 +203,7 @@ extern "C" int plbm_batch_create(int ngrids, const int* nx, const int* ny, const
     g.kind = kind[i];
     g.p = plbm_make_params(omega[i], trt_magic ? trt_magic[i] : 0.25);
     g.hp = hybrid_params(omega[i]);
+    g.ht = hybrid_trt_params(g.p);
     g.off = (long long)off;
     off += 2 * (size_t)g.ld * g.nx * 9;
     if (2 * (unsigned long long)g.ld * g.nx * 9 >= (1ull << 32)) b->small_index = 0;
@@ -285,7 +286,7 @@ extern "C" int plbm_batch_set_math(plbm_batch_t* b, int math) {
     return fail(PLBM_E_UNSUPPORTED, "PLBM_MATH_HYBRID needs PLBM_F64 storage");
   CUDA_TRY(cudaSetDevice(b->device), "cudaSetDevice");
   CUDA_TRY(cudaStreamSynchronize(b->stream), "synchronize");
-  for (BatchGrid& g : b->grids) g.hybrid = (math == PLBM_MATH_HYBRID && g.kind == PLBM_BGK) ? 1 : 0;
+  for (BatchGrid& g : b->grids) g.hybrid = math == PLBM_MATH_HYBRID ? 1 : 0;
   b->math = math;
   return apply_schedule(b);
 }

@@ -45,23 +45,47 @@ __device__ __forceinline__ E load_pop(const E* p) {
   else return __ldg(p);
 }
 
+// One binary64 cell outside the hybrid range: pull, the binary64 operator,
+// store.  Out of line so that the hot path's registers and code are not
+// shaped by this rarely taken path.  gp points at the grid's table entry.
+template <bool CG>
+__device__ __noinline__ void fallback_cell(const double* __restrict__ src, double* __restrict__ dst, int x, int y,
+                                           const BatchGrid* __restrict__ gp) {
+  const int nx = gp->nx, ny = gp->ny, ld = gp->ld;
+  double f[9];
+#pragma unroll
+  for (int q = 0; q < 9; q++) {
+    const int sx = wrap_add(x, -cx_of(q), nx), sy = wrap_add(y, -cy_of(q), ny);
+    f[q] = load_pop<CG>(src + YFast::off(sx, sy, q, nx, ny, ld));
+  }
+  if (gp->kind == K_TRT) collide_ref<K_TRT>(f, gp->p);
+  else collide_ref<K_BGK>(f, gp->p);
+#pragma unroll
+  for (int q = 0; q < 9; q++) dst[YFast::off(x, y, q, nx, ny, ld)] = f[q];
+}
+
 // Process one tile of one grid for one step.  I: index type inside one grid's
 // lattice pair (32-bit when every grid's pair has fewer than 2^32 elements).
+// gp is the grid's table entry; its relaxation constants are read where they
+// are used (through the read-only path) rather than held in registers.
 template <class S, bool CG, typename I>
-__device__ __forceinline__ void do_tile(const BatchGrid& g, int local_tile, int parity,
+__device__ __forceinline__ void do_tile(const BatchGrid* __restrict__ gp, int local_tile, int parity,
                                         typename S::elem* __restrict__ base) {
-  const int ty = g.ty;
+  const int nx = __ldg(&gp->nx), ny = __ldg(&gp->ny), ld = __ldg(&gp->ld);
+  const int ty = __ldg(&gp->ty);
   const int tx = blockDim.x / ty;
-  const int tiles_y = (g.ny + ty - 1) / ty;
+  const int tiles_y = (ny + ty - 1) / ty;
   const int txi = local_tile / tiles_y, tyi = local_tile - txi * tiles_y;
   const int y = tyi * ty + (int)(threadIdx.x % ty);
   const int x = txi * tx + (int)(threadIdx.x / ty);
-  if (x >= g.nx || y >= g.ny) return;
-  const I L = (I)g.ld, P = (I)g.ld * (I)g.nx, lat = 9 * P;
-  const typename S::elem* src = base + g.off + (parity ? lat : 0);
-  typename S::elem* dst = base + g.off + (parity ? 0 : lat);
-  const I c0 = (I)x * L, cm = (I)wrap_m(x, g.nx) * L, cp = (I)wrap_p(x, g.nx) * L;
-  const I y0 = (I)y, ym = (I)wrap_m(y, g.ny), yp = (I)wrap_p(y, g.ny);
+  if (x >= nx || y >= ny) return;
+  const int kind = __ldg(&gp->kind);
+  const long long goff = __ldg(&gp->off);
+  const I L = (I)ld, P = (I)ld * (I)nx, lat = 9 * P;
+  const typename S::elem* src = base + goff + (parity ? lat : 0);
+  typename S::elem* dst = base + goff + (parity ? 0 : lat);
+  const I c0 = (I)x * L, cm = (I)wrap_m(x, nx) * L, cp = (I)wrap_p(x, nx) * L;
+  const I y0 = (I)y, ym = (I)wrap_m(y, ny), yp = (I)wrap_p(y, ny);
   typedef typename S::elem E;
   E e[9];
   e[0] = load_pop<CG>(src + (c0 + y0));
@@ -77,24 +101,21 @@ __device__ __forceinline__ void do_tile(const BatchGrid& g, int local_tile, int 
 #pragma unroll
   for (int q = 0; q < 9; q++) f[q] = (typename S::real)e[q];
   if constexpr (S::ddf) {
-    if (g.kind == K_TRT) collide_shift<K_TRT, typename S::real>(f, g.p);
-    else collide_shift<K_BGK, typename S::real>(f, g.p);
+    if (kind == K_TRT) collide_shift<K_TRT, typename S::real>(f, gp->p);
+    else collide_shift<K_BGK, typename S::real>(f, gp->p);
   } else {
-    if (g.kind == K_TRT) {
-      collide_ref<K_TRT>(f, g.p);
-    } else if (g.hybrid) {
-      double keep[9];
-#pragma unroll
-      for (int q = 0; q < 9; q++) keep[q] = f[q];
+    if (__ldg(&gp->hybrid)) {
       bool bad = false;
-      hy::bgk_fast(f, g.hp, bad);
-      if (bad) {  // outside the hybrid range (|f| >= 2): straight binary64 BGK
-#pragma unroll
-        for (int q = 0; q < 9; q++) f[q] = keep[q];
-        collide_ref<K_BGK>(f, g.p);
+      if (kind == K_TRT) hy::trt_fast(f, gp->ht, bad);
+      else hy::bgk_fast(f, gp->hp, bad);
+      if (bad) {  // outside the hybrid range: the binary64 operator on the same inputs
+        fallback_cell<CG>(src, dst, x, y, gp);
+        return;
       }
+    } else if (kind == K_TRT) {
+      collide_ref<K_TRT>(f, gp->p);
     } else {
-      collide_ref<K_BGK>(f, g.p);
+      collide_ref<K_BGK>(f, gp->p);
     }
   }
   const I o = c0 + y0;
@@ -110,8 +131,7 @@ __device__ __forceinline__ void sweep(const BatchGrid* __restrict__ grids, const
                                       typename S::elem* base) {
   for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
     const int gi = __ldg(tile_grid + t);
-    const BatchGrid g = grids[gi];
-    do_tile<S, CG, I>(g, t - __ldg(tile_start + gi), parity, base);
+    do_tile<S, CG, I>(grids + gi, t - __ldg(tile_start + gi), parity, base);
   }
 }
 

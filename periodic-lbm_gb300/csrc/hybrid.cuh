@@ -1,26 +1,44 @@
-// hybrid.cuh -- binary64 BGK with the binary64 pipe reserved for the final
-// linear combination.
+// hybrid.cuh -- binary64 collisions with the binary64 pipe reserved for the
+// few operations that need its precision.
 //
 // GB300 issues binary64 at 1/64 of the binary32 rate, so a straight binary64
 // BGK (about 70 FP64 instructions per cell) is bound by the FP64 pipe at ~15 %
 // of HBM bandwidth.  This form keeps every term whose size is O(f) exact or
-// binary64, and moves the rest to integer and binary32 pipes:
+// binary64, and moves the rest to the integer and binary32 pipes.
 //
-//   F_q      = f_q * 2^59 as int64 (exact for f_q >= 2^-7; below that the
-//              truncation is < 2^-59)
-//   R, JX, JY = sum F_q, sum cx F_q, sum cy F_q         exact integer sums
-//   T_q      = R + 3 c_q.J                             exact integer
-//   corr_q   = omega w_q rho (4.5 (c_q.u)^2 - 1.5 u^2)  double-float, |corr| <~ 1e-3
+// Common part:
+//   F_q       = f_q * 2^59 as int64 (exact for |f_q| >= 2^-7; below that the
+//               truncation is < 2^-59)
+//   R, JX, JY = sum F_q, sum cx F_q, sum cy F_q          exact integer sums
+//
+// BGK (src/collision_bgk.F90:58-71, equilibrium src/fvm_bardow.F90:99-126):
+//   T_q      = R + 3 c_q.J                               exact integer
+//   corr_q   = omega w_q rho (4.5 (c_q.u)^2 - 1.5 u^2)   double-float, |corr| <~ 1e-3
 //   f'_q     = fma(omega w_q, T_q, fma(1 - omega, f_q, corr_q))   2 binary64 FMAs
+// which is f' = (1 - omega) f + omega feq with
+// feq_q = w_q (rho + 3 c.j + rho (4.5 (c.u)^2 - 1.5 u^2)), j = rho u.
 //
-// which is the BGK update f' = (1 - omega) f + omega feq with
-// feq_q = w_q rho (1 + 3 c.u + 4.5 (c.u)^2 - 1.5 u^2) written as
-// w_q (rho + 3 c.j + rho (4.5 (c.u)^2 - 1.5 u^2)), j = rho u
-// (src/collision_bgk.F90:58-71, src/fvm_bardow.F90:99-126).  Only corr_q is
-// evaluated in double-float; its size keeps the absolute error near 1e-18.
+// TRT, incompressible (src/collision_trt.F90:98-152): for a pair p, m = -p
+// with v = c_p.J,
+//   sym  = les (f_p + f_m - 2w rho) - les 2w (4.5 v^2 - 1.5 |j|^2)
+//   asym = lds (f_p - f_m - 6w v)
+//   f'_p = f_p - sym - asym,   f'_m = f_m - sym + asym
+// The linear brackets are exact integers up to a constant factor:
+//   9 (F_p + F_m) - 2 R   (axis, w = 1/9)    18 (F_p + F_m) - R  (diagonal)
+//   3 (F_p - F_m) - 2 V   (axis)             6 (F_p - F_m) - V   (diagonal)
+// so sym and asym -- the small non-equilibrium parts -- are evaluated in
+// double-float from exact inputs, and each population takes ONE binary64
+// addition: f'_p = f_p + (-sym - asym).  The rest population keeps
+// f'_0 = fma(1 - le, f_0, fma(le 4/9, R, -1.5 le 4/9 |j|^2)).
 //
-// Range: |f_q| < 2 for every population (so that the integer sums cannot
-// overflow); values outside it set the kernel's range flag.
+// Range.  The fast path takes |f_0| < 2, |f_axis| < 1/2, |f_diagonal| < 1/4
+// (biased binary64 exponent at most 1023, 1021, 1020).  Under these limits
+// every integer formed here stays below 16 * 2^59 < 2^63 in magnitude:
+// |R| < 5, |R + 3 c.J| < 11.5, |9 (F_p + F_m) - 2R| < 15,
+// |18 (F_p + F_m) - R| < 13, |3 (F_p - F_m) - 2V| < 3, |6 (F_p - F_m) - V| < 4
+// (in units of 2^59; each bound is the sum over q of |coefficient| x limit).
+// A cell with a population outside the limits reports `bad`; the kernels
+// then evaluate that cell with the binary64 operator instead.
 #pragma once
 #include "df64.cuh"
 
@@ -30,6 +48,9 @@ namespace hy {
 using df::df64;
 
 constexpr int kScale = 59;  // fixed-point scale 2^59
+
+// Largest biased binary64 exponent a population may have on the fast path.
+constexpr int kExpRest = 1023, kExpAxis = 1021, kExpDiag = 1020;
 
 DF_HD double fma_d(double a, double b, double c) {
 #ifdef __CUDA_ARCH__
@@ -48,11 +69,12 @@ DF_HD int clz64(uint64_t a) {
 }
 
 // binary64 -> int64 fixed point, scale 2^59, truncating toward zero.
-// `bad` is set when |d| >= 2 or d is not finite.
-DF_HD int64_t to_fixed(double d, bool& bad) {
+// `bad` is set when the biased exponent of d exceeds emax (emax <= 1023), or
+// d is not finite.
+DF_HD int64_t to_fixed_lim(double d, int emax, bool& bad) {
   const uint64_t u = df::d2u(d);
   const int e = (int)((u >> 52) & 0x7FF);
-  if (e >= 1024) {  // |d| >= 2, Inf, NaN
+  if (e > emax) {
     bad = true;
     return 0;
   }
@@ -105,46 +127,6 @@ DF_HD df64 fixed_to_df(int64_t T) {
   return df::make(hi, lo);
 }
 
-struct Params {
-  double omb;     // 1 - omega
-  double omw[3];  // omega * w for w0, ws, wd
-  df64 omw_df[3];  // the same as double-float
-};
-
-// One BGK collision of the 9 binary64 populations of a cell (in place).
-DF_HD void bgk(double (&f)[9], const Params& p, bool& bad) {
-  int64_t F[9];
-#pragma unroll
-  for (int q = 0; q < 9; q++) F[q] = to_fixed(f[q], bad);
-  const int64_t R = (((F[5] + F[7]) + (F[6] + F[8])) + ((F[1] + F[3]) + (F[2] + F[4]))) + F[0];
-  const int64_t d57 = F[5] - F[7], d86 = F[8] - F[6];
-  const int64_t JX = (d57 + d86) + (F[1] - F[3]);
-  const int64_t JY = (d57 - d86) + (F[2] - F[4]);
-  // nonlinear part in double-float
-  const df64 rho = fixed_to_df(R);
-  const df64 inv = df::recip(rho);
-  const df64 ux = df::mul(fixed_to_df(JX), inv), uy = df::mul(fixed_to_df(JY), inv);
-  const df64 u2_15 = df::mul_f(df::add(df::sqr(ux), df::sqr(uy)), 1.5f);
-  // q = 0: corr = omega w0 rho (-1.5 u^2)
-  {
-    const double c0 = df::pack_double(df::neg(df::mul(p.omw_df[0], df::mul(rho, u2_15))));
-    f[0] = fma_d(p.omw[0], fixed_to_double(R), fma_d(p.omb, f[0], c0));
-  }
-#define PLBM_HY_PAIR(QP, QM, CU, CJ, WI)                                                    \
-  {                                                                                         \
-    const double c = df::pack_double(                                                       \
-        df::mul(p.omw_df[WI], df::mul(rho, df::sub(df::mul_f(df::sqr(CU), 4.5f), u2_15))));  \
-    const int64_t cj3 = (CJ) + ((CJ) << 1);                                                 \
-    f[QP] = fma_d(p.omw[WI], fixed_to_double(R + cj3), fma_d(p.omb, f[QP], c));             \
-    f[QM] = fma_d(p.omw[WI], fixed_to_double(R - cj3), fma_d(p.omb, f[QM], c));             \
-  }
-  PLBM_HY_PAIR(1, 3, ux, JX, 1)
-  PLBM_HY_PAIR(2, 4, uy, JY, 1)
-  PLBM_HY_PAIR(5, 7, df::add(ux, uy), JX + JY, 2)
-  PLBM_HY_PAIR(8, 6, df::sub(ux, uy), JX - JY, 2)
-#undef PLBM_HY_PAIR
-}
-
 // ---- fast paths for the ranges lattice states live in --------------------
 // The general conversions are called out of line from the fast paths, so that
 // the compiler branches around them instead of predicating them in.
@@ -153,9 +135,9 @@ DF_HD void bgk(double (&f)[9], const Params& p, bool& bad) {
 #else
 #define PLBM_NOINLINE static __attribute__((noinline))
 #endif
-PLBM_NOINLINE int64_t to_fixed_slow(double d, int* bad) {
+PLBM_NOINLINE int64_t to_fixed_slow(double d, int emax, int* bad) {
   bool b = false;
-  const int64_t r = to_fixed(d, b);
+  const int64_t r = to_fixed_lim(d, emax, b);
   if (b) *bad = 1;
   return r;
 }
@@ -170,20 +152,36 @@ DF_HD uint32_t funnel_l(uint32_t lo, uint32_t hi, uint32_t sh) {
 #endif
 }
 
-// to_fixed for positive f in [2^-7, 2): one 64-bit shift by 0..7, the same
-// exact value as the general conversion (which handles everything else).
+// to_fixed_lim for positive f in [2^-7, 2^(EMAX-1022)): one 64-bit shift by
+// 0..EMAX-1016, the same exact value as the general conversion (which handles
+// everything else).
+template <int EMAX>
 DF_HD int64_t to_fixed_fast(double d, bool& bad) {
+  static_assert(EMAX >= 1016 && EMAX <= 1023, "fast-path exponent range");
   const uint64_t u = df::d2u(d);
   const uint32_t H = (uint32_t)(u >> 32), L = (uint32_t)u;
   const uint32_t sh = (H >> 20) - 1016u;  // a set sign bit makes this large
-  if (sh <= 7u) {
+  if (sh <= (uint32_t)(EMAX - 1016)) {
     const uint32_t mh = (H & 0xFFFFFu) | 0x100000u;
     return (int64_t)(((uint64_t)funnel_l(L, mh, sh) << 32) | (uint64_t)(L << sh));
   }
   int b = 0;
-  const int64_t r = to_fixed_slow(d, &b);
+  const int64_t r = to_fixed_slow(d, EMAX, &b);
   if (b) bad = true;
   return r;
+}
+
+// The nine populations of a cell under the fast-path limits.
+DF_HD void load_fixed(const double (&f)[9], int64_t (&F)[9], bool& bad) {
+  F[0] = to_fixed_fast<kExpRest>(f[0], bad);
+  F[1] = to_fixed_fast<kExpAxis>(f[1], bad);
+  F[2] = to_fixed_fast<kExpAxis>(f[2], bad);
+  F[3] = to_fixed_fast<kExpAxis>(f[3], bad);
+  F[4] = to_fixed_fast<kExpAxis>(f[4], bad);
+  F[5] = to_fixed_fast<kExpDiag>(f[5], bad);
+  F[6] = to_fixed_fast<kExpDiag>(f[6], bad);
+  F[7] = to_fixed_fast<kExpDiag>(f[7], bad);
+  F[8] = to_fixed_fast<kExpDiag>(f[8], bad);
 }
 
 // fixed_to_double for 2^58 <= T < 2^60 (values in [0.5, 2)): a shift by 6 or
@@ -204,12 +202,17 @@ DF_HD double fixed_to_double_fast(int64_t T) {
   return fixed_to_double_slow(T);
 }
 
-// BGK of the hybrid arithmetic with the fast conversions: the same update as
-// bgk() (rho for the nonlinear term taken from the rounded binary64 R).
+struct Params {
+  double omb;     // 1 - omega
+  double omw[3];  // omega * w for w0, ws, wd
+  df64 omw_df[3];  // the same as double-float
+};
+
+// BGK in the hybrid arithmetic (in place).  On `bad` the populations are
+// left in an unspecified state: the caller evaluates the cell another way.
 DF_HD void bgk_fast(double (&f)[9], const Params& p, bool& bad) {
   int64_t F[9];
-#pragma unroll
-  for (int q = 0; q < 9; q++) F[q] = to_fixed_fast(f[q], bad);
+  load_fixed(f, F, bad);
   const int64_t R = (((F[5] + F[7]) + (F[6] + F[8])) + ((F[1] + F[3]) + (F[2] + F[4]))) + F[0];
   const int64_t d57 = F[5] - F[7], d86 = F[8] - F[6];
   const int64_t JX = (d57 + d86) + (F[1] - F[3]);
@@ -227,7 +230,7 @@ DF_HD void bgk_fast(double (&f)[9], const Params& p, bool& bad) {
   {                                                                                         \
     const double c = df::pack_double(                                                       \
         df::mul(p.omw_df[WI], df::mul(rho, df::sub(df::mul_f(df::sqr(CU), 4.5f), u2_15))));  \
-    const int64_t cj3 = (CJ) + ((CJ) << 1);                                                 \
+    const int64_t cj3 = 3 * (CJ);                                                           \
     f[QP] = fma_d(p.omw[WI], fixed_to_double_fast(R + cj3), fma_d(p.omb, f[QP], c));        \
     f[QM] = fma_d(p.omw[WI], fixed_to_double_fast(R - cj3), fma_d(p.omb, f[QM], c));        \
   }
@@ -236,6 +239,60 @@ DF_HD void bgk_fast(double (&f)[9], const Params& p, bool& bad) {
   PLBM_HY_PAIR(5, 7, df::add(ux, uy), JX + JY, 2)
   PLBM_HY_PAIR(8, 6, df::sub(ux, uy), JX - JY, 2)
 #undef PLBM_HY_PAIR
+}
+
+// Incompressible TRT constants (index 0: axis pairs, 1: diagonal pairs).
+struct TrtParams {
+  double omb;      // 1 - lambda_e
+  double le_t0;    // lambda_e * 4/9
+  df64 nl0;        // -1.5 lambda_e 4/9: coefficient of |j|^2 in f'_0
+  df64 cs[2];      // les / 9, les / 18: coefficient of the exact symmetric bracket
+  df64 cd[2];      // lds / 3, lds / 6: coefficient of the exact antisymmetric bracket
+  df64 c4[2];      // les 2w 4.5: coefficient of v^2 in sym
+  df64 c1[2];      // les 2w 1.5: coefficient of |j|^2 in sym
+};
+
+// TRT in the hybrid arithmetic (in place); `bad` as for bgk_fast.
+DF_HD void trt_fast(double (&f)[9], const TrtParams& p, bool& bad) {
+  int64_t F[9];
+  load_fixed(f, F, bad);
+  const int64_t R = (((F[5] + F[7]) + (F[6] + F[8])) + ((F[1] + F[3]) + (F[2] + F[4]))) + F[0];
+  const int64_t d57 = F[5] - F[7], d86 = F[8] - F[6];
+  const int64_t JX = (d57 + d86) + (F[1] - F[3]);
+  const int64_t JY = (d57 - d86) + (F[2] - F[4]);
+  const df64 jx = fixed_to_df(JX), jy = fixed_to_df(JY);
+  const df64 j2 = df::add(df::sqr(jx), df::sqr(jy));
+  {
+    const double c0 = df::pack_double(df::mul(p.nl0, j2));
+    f[0] = fma_d(p.omb, f[0], fma_d(p.le_t0, fixed_to_double_fast(R), c0));
+  }
+  const df64 c1j2[2] = {df::mul(p.c1[0], j2), df::mul(p.c1[1], j2)};
+  // MS, MD: the exact brackets of the pair; VDF = c_p.j
+#define PLBM_HY_TRT_PAIR(QP, QM, VDF, MS, MD, A)                                            \
+  {                                                                                         \
+    const df64 sym = df::sub(df::mul(p.cs[A], fixed_to_df(MS)),                             \
+                             df::sub(df::mul(p.c4[A], df::sqr(VDF)), c1j2[A]));             \
+    const df64 asym = df::mul(p.cd[A], fixed_to_df(MD));                                    \
+    f[QP] = f[QP] + df::pack_double(df::neg(df::add(sym, asym)));                           \
+    f[QM] = f[QM] + df::pack_double(df::sub(asym, sym));                                    \
+  }
+  {
+    const int64_t s = F[1] + F[3], d = F[1] - F[3];
+    PLBM_HY_TRT_PAIR(1, 3, jx, 9 * s - 2 * R, 3 * d - 2 * JX, 0)
+  }
+  {
+    const int64_t s = F[2] + F[4], d = F[2] - F[4];
+    PLBM_HY_TRT_PAIR(2, 4, jy, 9 * s - 2 * R, 3 * d - 2 * JY, 0)
+  }
+  {
+    const int64_t s = F[5] + F[7], d = F[5] - F[7];
+    PLBM_HY_TRT_PAIR(5, 7, df::add(jx, jy), 18 * s - R, 6 * d - (JX + JY), 1)
+  }
+  {
+    const int64_t s = F[8] + F[6], d = F[8] - F[6];
+    PLBM_HY_TRT_PAIR(8, 6, df::sub(jx, jy), 18 * s - R, 6 * d - (JX - JY), 1)
+  }
+#undef PLBM_HY_TRT_PAIR
 }
 
 }  // namespace hy

@@ -13,15 +13,17 @@ constexpr int kBatchMaxThreads = 512;
 struct alignas(16) BatchGrid {
   CollParams p;       // relaxation parameters (grid's omega / TRT magic)
   hy::Params hp;      // the same for the hybrid binary64 BGK
+  hy::TrtParams ht;   // ... and TRT
   long long off;      // element offset of lattice A; lattice B follows it
   int nx, ny, ld;
   int kind;           // K_BGK or K_TRT
   int ty;             // tile rows along y; tile columns = threads / ty
-  int hybrid;         // binary64 BGK in hybrid arithmetic
+  int hybrid;         // binary64 grid in hybrid arithmetic
   int pad[2];
 };
 
 hy::Params hybrid_params(double omega);
+hy::TrtParams hybrid_trt_params(const CollParams& p);
 
 struct BatchLaunch {
   const BatchGrid* grids;  // device

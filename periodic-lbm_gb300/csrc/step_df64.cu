@@ -1,6 +1,8 @@
 // step_df64.cu -- binary64-storage fused step in the "hybrid" arithmetic of
-// hybrid.cuh (exact integer moments, double-float nonlinear term, binary64
-// FMAs for the final linear combination).  BGK only.
+// hybrid.cuh (exact integer moments, double-float small terms, binary64 only
+// for the final combination), BGK and TRT.  Cells outside the hybrid range
+// are evaluated with the binary64 operator of the reference (and set the
+// range flag).
 //
 // Also the deviation-storage steps whose collision runs in more than binary32:
 // double-float (PLBM_MATH_HYBRID) or binary64 (PLBM_MATH_STRICT) arithmetic on
@@ -81,13 +83,38 @@ df::df64 split_const(double d) {
   return df::make(hi, (float)(d - (double)hi));
 }
 
+// Constants of one hybrid launch: the hybrid operator's and the binary64
+// operator's (for cells outside the hybrid range).
+struct HybridArgs {
+  hy::Params bgk;
+  hy::TrtParams trt;
+  CollParams ref;
+};
+
+// One cell outside the hybrid range: pull, the binary64 operator of the
+// reference, store.  Out of line so that the hot kernel's registers and code
+// are not shaped by this rarely taken path.
+template <int KIND>
+__device__ __noinline__ void hybrid_fallback_cell(const double* __restrict__ src, double* __restrict__ dst, int x,
+                                                  int y, int nx, int ny, int ld, const CollParams& p) {
+  double f[9];
+#pragma unroll
+  for (int q = 0; q < 9; q++) {
+    const int sx = wrap_add(x, -cx_of(q), nx), sy = wrap_add(y, -cy_of(q), ny);
+    f[q] = src[YFast::off(sx, sy, q, nx, ny, ld)];
+  }
+  collide_ref<KIND>(f, p);
+#pragma unroll
+  for (int q = 0; q < 9; q++) dst[YFast::off(x, y, q, nx, ny, ld)] = f[q];
+  g_hybrid_range_flag = 1;
+}
+
 // I: index type of the lattice offsets; 32-bit when the whole lattice has
 // fewer than 2^32 elements (one multiply-add per address instead of 64-bit
 // arithmetic).
-template <typename I>
-__global__ void __launch_bounds__(kBlock) k_step_hybrid_bgk(const double* __restrict__ src,
-                                                           double* __restrict__ dst, int nx, int ny, int ld,
-                                                           int ftiles, hy::Params p) {
+template <typename I, int KIND>
+__global__ void __launch_bounds__(kBlock) k_step_hybrid(const double* __restrict__ src, double* __restrict__ dst,
+                                                       int nx, int ny, int ld, int ftiles, HybridArgs a) {
   const int x = blockIdx.x / ftiles;
   const int y = (blockIdx.x - x * ftiles) * blockDim.x + threadIdx.x;
   if (y >= ny) return;
@@ -106,11 +133,26 @@ __global__ void __launch_bounds__(kBlock) k_step_hybrid_bgk(const double* __rest
   f[7] = __ldg(src + (7 * P + cp + yp));
   f[8] = __ldg(src + (8 * P + cm + yp));
   bool bad = false;
-  hy::bgk_fast(f, p, bad);
-  if (bad) g_hybrid_range_flag = 1;
+  if (KIND == K_TRT) hy::trt_fast(f, a.trt, bad);
+  else hy::bgk_fast(f, a.bgk, bad);
+  if (bad) {  // outside the hybrid range: the binary64 operator on the same inputs
+    hybrid_fallback_cell<KIND>(src, dst, x, y, nx, ny, ld, a.ref);
+    return;
+  }
   const I o = c0 + y0;
 #pragma unroll
   for (int q = 0; q < 9; q++) dst[(I)q * P + o] = f[q];
+}
+
+template <int KIND>
+cudaError_t launch_hybrid(const Sweep& s, unsigned blocks, int ft, const HybridArgs& a) {
+  const double* src = static_cast<const double*>(s.src);
+  double* dst = static_cast<double*>(s.dst);
+  if ((unsigned long long)s.ld * (unsigned long long)s.nx * 9ull < (1ull << 32))
+    k_step_hybrid<uint32_t, KIND><<<blocks, kBlock, 0, s.stream>>>(src, dst, s.nx, s.ny, s.ld, ft, a);
+  else
+    k_step_hybrid<size_t, KIND><<<blocks, kBlock, 0, s.stream>>>(src, dst, s.nx, s.ny, s.ld, ft, a);
+  return cudaGetLastError();
 }
 
 }  // namespace
@@ -121,26 +163,41 @@ hy::Params hybrid_params(double omega) {
   const double w[3] = {W0, WS, WD};
   for (int i = 0; i < 3; i++) {
     p.omw[i] = omega * w[i];
-    const float hi = (float)p.omw[i];
-    p.omw_df[i] = df::make(hi, (float)(p.omw[i] - (double)hi));
+    p.omw_df[i] = split_const(p.omw[i]);
   }
   return p;
 }
 
+// Constants of the hybrid TRT from the launch's binary64 parameters
+// (le = omega, les = omega/2, lds = lambda_d/2 as the reference forms them).
+hy::TrtParams hybrid_trt_params(const CollParams& cp) {
+  hy::TrtParams p;
+  const double le = cp.omega, les = cp.les, lds = cp.lds;
+  p.omb = 1.0 - le;
+  p.le_t0 = le * TRT_T0;
+  p.nl0 = split_const(-1.5 * p.le_t0);
+  p.cs[0] = split_const(les / 9.0);
+  p.cs[1] = split_const(les / 18.0);
+  p.cd[0] = split_const(lds / 3.0);
+  p.cd[1] = split_const(lds / 6.0);
+  p.c4[0] = split_const(les);          // les 2 (1/9) 4.5
+  p.c4[1] = split_const(les / 4.0);    // les 2 (1/36) 4.5
+  p.c1[0] = split_const(les / 3.0);    // les 2 (1/9) 1.5
+  p.c1[1] = split_const(les / 12.0);   // les 2 (1/36) 1.5
+  return p;
+}
+
 cudaError_t step_pull_df64(int kind, const Sweep& s, const CollParams& cp) {
-  if (kind != K_BGK) return cudaErrorNotSupported;
+  if (kind != K_BGK && kind != K_TRT) return cudaErrorNotSupported;
   const int ft = (s.ny + kBlock - 1) / kBlock;
   const long long blocks = (long long)ft * s.nx;
   if (blocks <= 0 || blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
-  const double* a = static_cast<const double*>(s.src);
-  double* b = static_cast<double*>(s.dst);
-  if ((unsigned long long)s.ld * (unsigned long long)s.nx * 9ull < (1ull << 32))
-    k_step_hybrid_bgk<uint32_t><<<(unsigned)blocks, kBlock, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft,
-                                                                           hybrid_params(cp.omega));
-  else
-    k_step_hybrid_bgk<size_t><<<(unsigned)blocks, kBlock, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft,
-                                                                         hybrid_params(cp.omega));
-  return cudaGetLastError();
+  HybridArgs a;
+  a.bgk = hybrid_params(cp.omega);
+  a.trt = hybrid_trt_params(cp);
+  a.ref = cp;
+  if (kind == K_TRT) return launch_hybrid<K_TRT>(s, (unsigned)blocks, ft, a);
+  return launch_hybrid<K_BGK>(s, (unsigned)blocks, ft, a);
 }
 
 cudaError_t step_pull_dev_hi(int storage, int math, int kind, const Sweep& s, const CollParams& cp) {

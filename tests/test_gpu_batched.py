@@ -171,11 +171,13 @@ def test_batched_hybrid_matches_oracle_per_grid(gpu_lib):
     p.close()
 
 
-def test_batched_hybrid_falls_back_outside_range(gpu_lib):
-    """A BGK grid holding |f| >= 2 takes the FMA BGK in those cells: the
-    result equals the FMA batch's to 1e-12."""
+@pytest.mark.parametrize("kind", ["bgk", "trt"])
+def test_batched_hybrid_falls_back_outside_range(gpu_lib, kind):
+    """A grid holding populations past the hybrid limits (f_0 >= 2) takes the
+    FMA binary64 operator in those cells: the result equals the FMA batch's
+    to 1e-12."""
     from plbm.batched import BatchedGrids, GridSpec
-    specs = [GridSpec(16, 32, "bgk", 1.3)]
+    specs = [GridSpec(16, 32, kind, 1.3)]
     rng = np.random.default_rng(9)
     rho = 5.0 + 0.01 * rng.standard_normal((16, 32))  # f_0 = 4/9 rho > 2
     ux = 0.02 * rng.standard_normal((16, 32))

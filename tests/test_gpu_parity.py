@@ -80,24 +80,53 @@ def test_fused_step_fma_within_1e12(gpu_lib, nx, ny, kind, omega):
     g.close()
 
 
+def hybrid_flag(reset=1):
+    import ctypes as C
+    from plbm import _lib
+    flag = C.c_int(-1)
+    _lib.check(_lib.load().plbm_hybrid_range_flag(C.byref(flag), reset))
+    return flag.value
+
+
+@pytest.mark.parametrize("kind", ["bgk", "trt"])
 @pytest.mark.parametrize("nx,ny,steps,omega", [(17, 13, 10, 1.25), (64, 64, 1000, 1.6), (64, 64, 1000, 1.9),
                                                (256, 192, 200, 1.25), (33, 48, 500, 1.8)])
-def test_hybrid_bgk_within_1e12(gpu_lib, nx, ny, steps, omega):
-    """PLBM_MATH_HYBRID (exact integer moments, double-float nonlinear term,
-    binary64 FMA relaxation) against the oracle at the binary64 tolerance."""
+def test_hybrid_within_1e12(gpu_lib, kind, nx, ny, steps, omega):
+    """PLBM_MATH_HYBRID (exact integer moments, double-float small terms,
+    binary64 for the final combination) against the oracle at the binary64
+    tolerance; near-equilibrium states never leave the hybrid range."""
+    hybrid_flag()
     f0 = initial_state(nx, ny)
-    ref, iold, _ = oracle_steps(f0, ny, "bgk", omega, 0.25, steps)
-    g = gpu_steps(f0, nx, ny, "bgk", omega, 0.25, steps, "hybrid")
+    ref, iold, _ = oracle_steps(f0, ny, kind, omega, 0.25, steps)
+    g = gpu_steps(f0, nx, ny, kind, omega, 0.25, steps, "hybrid")
     got = g.download(g.iold)
     r_ref = O.update_macros(ref[iold - 1], ny)
     r_got = O.update_macros(got, ny)
     for a, b in zip(r_got, r_ref):
         assert relinf(a, b) <= TOL
-    from plbm import _lib
-    import ctypes as C
-    flag = C.c_int(-1)
-    _lib.check(_lib.load().plbm_hybrid_range_flag(C.byref(flag), 1))
-    assert flag.value == 0
+    assert hybrid_flag() == 0
+    g.close()
+
+
+@pytest.mark.parametrize("kind", ["bgk", "trt"])
+@pytest.mark.parametrize("rho0", [5.0, 2.5])
+def test_hybrid_out_of_range_cells_fall_back(gpu_lib, kind, rho0):
+    """Cells with populations past the hybrid limits (|f_0| >= 2 at rho0 = 5;
+    |f_axis| >= 1/2 where c.u is large at rho0 = 2.5) are evaluated with the
+    binary64 operator: the result still meets the binary64 tolerance and the
+    flag reports the fallback."""
+    nx, ny = 32, 24
+    rng = np.random.default_rng(5)
+    rho = rho0 * (1.0 + 0.05 * rng.standard_normal((nx, ny)))
+    ux = 0.15 * rng.standard_normal((nx, ny))
+    uy = 0.15 * rng.standard_normal((nx, ny))
+    f0 = O.set_pdf_to_equilibrium(rho, ux, uy)
+    hybrid_flag()
+    ref, iold, _ = oracle_steps(f0, ny, kind, 1.3, 0.25, 4)
+    g = gpu_steps(f0, nx, ny, kind, 1.3, 0.25, 4, "hybrid")
+    got = g.download(g.iold)
+    assert relinf(got[:, :, :ny], ref[iold - 1][:, :, :ny]) <= TOL
+    assert hybrid_flag() == 1
     g.close()
 
 
@@ -121,7 +150,7 @@ def test_hybrid_long_horizon_bench_state(gpu_lib):
 
 def test_hybrid_rejects_other_collisions(gpu_lib):
     from plbm import LatticeGrid, PlbmError
-    g = LatticeGrid(16, 16, collision="trt", math="hybrid")
+    g = LatticeGrid(16, 16, collision="rr", math="hybrid")
     with pytest.raises(PlbmError) as e:
         g.perform_lbm_step(1)
     assert e.value.code == -4
