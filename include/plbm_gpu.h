@@ -47,11 +47,12 @@ extern "C" {
  *   FMA    binary64, FMA contraction allowed (default)
  *   STRICT binary64, no contraction: the Fortran's operations in its order,
  *          bit-identical to it
- *   HYBRID BGK and TRT: exact integer moments, double-float for the small
- *          terms, binary64 only for the final combination (BGK: 18 FP64
- *          instructions per cell instead of ~70; TRT: 10).  A cell with
- *          |f_0| >= 2, |f_axis| >= 1/2 or |f_diagonal| >= 1/4 is evaluated
- *          with the FMA binary64 operator instead (see plbm_hybrid_range_flag)
+ *   HYBRID BGK, TRT and RR: exact integer moments, double-float for the
+ *          small terms, binary64 only for the final combination (FP64
+ *          instructions per cell: BGK 18, TRT 10, RR 9, instead of 60-150).
+ *          A cell with |f_0| >= 2, |f_axis| >= 1/2 or |f_diagonal| >= 1/4
+ *          is evaluated with the FMA binary64 operator instead (see
+ *          plbm_hybrid_range_flag)
  * Deviation storage (PLBM_F32DEV / PLBM_F16DEV):
  *   FMA    binary32 collision (default)
  *   STRICT binary64 collision on the stored deviations

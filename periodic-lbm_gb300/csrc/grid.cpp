@@ -392,8 +392,8 @@ extern "C" int plbm_collide(plbm_grid_t* g) {
 extern "C" int plbm_perform_lbm_step(plbm_grid_t* g, int nsteps) {
   if (int r = check_grid(g)) return r;
   if (nsteps < 0) return fail(PLBM_E_INVALID, "nsteps = %d < 0", nsteps);
-  if (g->storage == PLBM_F64 && g->math == PLBM_MATH_HYBRID && g->kind != PLBM_BGK && g->kind != PLBM_TRT)
-    return fail(PLBM_E_UNSUPPORTED, "PLBM_MATH_HYBRID with PLBM_F64 storage is offered for collide_bgk and collide_trt");
+  if (g->storage == PLBM_F64 && g->math == PLBM_MATH_HYBRID && g->kind == PLBM_BGKI)
+    return fail(PLBM_E_UNSUPPORTED, "PLBM_MATH_HYBRID is not offered for collide_bgk_improved");
   if (g->storage != PLBM_F64 && (g->math == PLBM_MATH_HYBRID || g->math == PLBM_MATH_DF64) && g->kind != PLBM_BGK)
     return fail(PLBM_E_UNSUPPORTED, "PLBM_MATH_HYBRID / PLBM_MATH_DF64 with deviation storage are offered for collide_bgk only");
   if (int r = use_device(g)) return r;
@@ -540,8 +540,8 @@ extern "C" int plbm_launch_step(int storage, int math, int kind, int nx, int ny,
   if (storage == PLBM_F64) {
     if (kind == PLBM_BGKI && ld != ny)
       return fail(PLBM_E_UNSUPPORTED, "fused collide_bgk_improved needs ld == ny");
-    if (math == PLBM_MATH_HYBRID && kind != PLBM_BGK && kind != PLBM_TRT)
-      return fail(PLBM_E_UNSUPPORTED, "PLBM_MATH_HYBRID is offered for collide_bgk and collide_trt");
+    if (math == PLBM_MATH_HYBRID && kind == PLBM_BGKI)
+      return fail(PLBM_E_UNSUPPORTED, "PLBM_MATH_HYBRID is not offered for collide_bgk_improved");
     if (math == PLBM_MATH_STRICT) e = strict::step_pull_f64(kind, s, p);
     else if (math == PLBM_MATH_HYBRID) e = step_pull_df64(kind, s, p);
     else e = fma::step_pull_f64(kind, s, p);

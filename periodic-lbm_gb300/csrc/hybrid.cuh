@@ -295,5 +295,88 @@ DF_HD void trt_fast(double (&f)[9], const TrtParams& p, bool& bad) {
 #undef PLBM_HY_TRT_PAIR
 }
 
+// Recursive-regularized constants.
+struct RrParams {
+  double w[3];   // 4/9, 1/9, 1/36 in binary64 (final FMA)
+  df64 wdf[3];   // the same as double-float
+  df64 omb;      // 1 - omega
+  df64 third;    // 1/3
+};
+
+// Recursive regularized collision (src/collision_regularized.F90:72-194) in
+// the hybrid arithmetic (in place); `bad` as for bgk_fast.
+//   f'_q = feq_q + w_q (1 - omega) H_q(a)
+// with feq_q = w_q (T_q + rho NL_q(u)), T_q = R + 3 c_q.J exact, NL_q the
+// second-, third- and fourth-order Hermite terms of the reference's
+// equilibrium, and the non-equilibrium second moments evaluated from exact
+// integer moments: the equilibrium's second moments are rho u u + rho/3 I
+// (the third- and fourth-order Hermite terms are orthogonal to them on D2Q9),
+// so
+//   a_xx = (3 Pxx - R)/3 - jx ux,  a_yy = (3 Pyy - R)/3 - jy uy,
+//   a_xy = Pxy - jx uy,
+// Pxx = sum cx^2 F, Pyy = sum cy^2 F, Pxy = sum cx cy F.  One binary64 FMA per
+// population: f'_q = fma(w_q, T_q, w_q (rho NL_q + (1 - omega) H_q)).
+DF_HD void rr_fast(double (&f)[9], const RrParams& p, bool& bad) {
+  using namespace df;
+  int64_t F[9];
+  load_fixed(f, F, bad);
+  const int64_t s57 = F[5] + F[7], s68 = F[6] + F[8];
+  const int64_t sd = s57 + s68;
+  const int64_t R = ((s57 + s68) + ((F[1] + F[3]) + (F[2] + F[4]))) + F[0];
+  const int64_t d57 = F[5] - F[7], d86 = F[8] - F[6];
+  const int64_t JX = (d57 + d86) + (F[1] - F[3]);
+  const int64_t JY = (d57 - d86) + (F[2] - F[4]);
+  const int64_t PXX3 = 3 * ((F[1] + F[3]) + sd) - R;
+  const int64_t PYY3 = 3 * ((F[2] + F[4]) + sd) - R;
+  const int64_t PXY = s57 - s68;
+  const double Rd = fixed_to_double_fast(R);
+  const df64 rho = from_double(Rd);
+  const df64 inv = recip(rho);
+  const df64 jx = fixed_to_df(JX), jy = fixed_to_df(JY);
+  const df64 ux = mul(jx, inv), uy = mul(jy, inv);
+  const df64 uxx = sqr(ux), uyy = sqr(uy);
+  const df64 uxxy = mul(uxx, uy), uyyx = mul(uyy, ux), uxxyy = mul(uxx, uyy);
+  // non-equilibrium second moments
+  const df64 axx = sub(mul(fixed_to_df(PXX3), p.third), mul(jx, ux));
+  const df64 ayy = sub(mul(fixed_to_df(PYY3), p.third), mul(jy, uy));
+  const df64 axy = sub(fixed_to_df(PXY), mul(jx, uy));
+  // recursive third and fourth order
+  const df64 axxy = add(mul_pow2(mul(ux, axy), 2.0f), mul(uy, axx));
+  const df64 ayyx = add(mul_pow2(mul(uy, axy), 2.0f), mul(ux, ayy));
+  const df64 axxyy = sub(sub(sub(mul_pow2(add(mul(ux, ayyx), mul(uy, axxy)), 2.0f), mul(uxx, ayy)), mul(uyy, axx)),
+                         mul_pow2(mul(mul(ux, uy), axy), 4.0f));
+  const df64 i0 = mul_f(add(axx, ayy), -1.5f);
+  const df64 is = sub(i0, mul_f(axxyy, 4.5f));
+  const df64 id = sub(mul_f(axxyy, 9.0f), mul_pow2(i0, 2.0f));
+  // equilibrium nonlinear terms
+  const df64 base = mul_f(add(uxx, uyy), -1.5f);
+  const df64 nls = sub(base, mul_f(uxxyy, 4.5f));
+  const df64 nld = add(base, mul_f(uxxyy, 9.0f));
+  {
+    const df64 nl0 = add(base, mul_f(uxxyy, 2.25f));
+    const df64 h0 = add(i0, mul_f(axxyy, 2.25f));
+    const df64 b0 = add(mul(rho, nl0), mul(p.omb, h0));
+    f[0] = fma_d(p.w[0], Rd, pack_double(mul(p.wdf[0], b0)));
+  }
+  // pair p, m: NL = A +- B, H = C +- D, T = R +- 3 CJ
+#define PLBM_HY_RR_PAIR(QP, QM, A, B, C, D, CJ, WI)                                           \
+  {                                                                                           \
+    const df64 X = add(mul(rho, (A)), mul(p.omb, (C)));                                       \
+    const df64 Y = add(mul(rho, (B)), mul(p.omb, (D)));                                       \
+    const int64_t cj3 = 3 * (CJ);                                                             \
+    f[QP] = fma_d(p.w[WI], fixed_to_double_fast(R + cj3), pack_double(mul(p.wdf[WI], add(X, Y)))); \
+    f[QM] = fma_d(p.w[WI], fixed_to_double_fast(R - cj3), pack_double(mul(p.wdf[WI], sub(X, Y)))); \
+  }
+  PLBM_HY_RR_PAIR(1, 3, add(nls, mul_f(uxx, 4.5f)), mul_f(uyyx, -4.5f), add(is, mul_f(axx, 4.5f)),
+                  mul_f(ayyx, -4.5f), JX, 1)
+  PLBM_HY_RR_PAIR(2, 4, add(nls, mul_f(uyy, 4.5f)), mul_f(uxxy, -4.5f), add(is, mul_f(ayy, 4.5f)),
+                  mul_f(axxy, -4.5f), JY, 1)
+  PLBM_HY_RR_PAIR(5, 7, add(nld, mul_f(sqr(add(ux, uy)), 4.5f)), mul_f(add(uxxy, uyyx), 9.0f),
+                  add(id, mul_f(axy, 9.0f)), mul_f(add(axxy, ayyx), 9.0f), JX + JY, 2)
+  PLBM_HY_RR_PAIR(6, 8, add(nld, mul_f(sqr(sub(ux, uy)), 4.5f)), mul_f(sub(uxxy, uyyx), 9.0f),
+                  sub(id, mul_f(axy, 9.0f)), mul_f(sub(axxy, ayyx), 9.0f), JY - JX, 2)
+#undef PLBM_HY_RR_PAIR
+}
+
 }  // namespace hy
 }  // namespace plbm

@@ -35,7 +35,7 @@ PLBM_DECLARE_F64(fma)
 PLBM_DECLARE_F64(strict)
 #undef PLBM_DECLARE_F64
 
-// binary64 storage, hybrid arithmetic (hybrid.cuh), YFast pull, BGK and TRT
+// binary64 storage, hybrid arithmetic (hybrid.cuh), YFast pull, BGK, TRT and RR
 cudaError_t step_pull_df64(int kind, const Sweep& s, const CollParams& p);
 cudaError_t hybrid_range_flag(int* flag, int reset);
 

@@ -1,6 +1,6 @@
 // step_df64.cu -- binary64-storage fused step in the "hybrid" arithmetic of
 // hybrid.cuh (exact integer moments, double-float small terms, binary64 only
-// for the final combination), BGK and TRT.  Cells outside the hybrid range
+// for the final combination), BGK, TRT and RR.  Cells outside the hybrid range
 // are evaluated with the binary64 operator of the reference (and set the
 // range flag).
 //
@@ -88,6 +88,7 @@ df::df64 split_const(double d) {
 struct HybridArgs {
   hy::Params bgk;
   hy::TrtParams trt;
+  hy::RrParams rr;
   CollParams ref;
 };
 
@@ -134,6 +135,7 @@ __global__ void __launch_bounds__(kBlock) k_step_hybrid(const double* __restrict
   f[8] = __ldg(src + (8 * P + cm + yp));
   bool bad = false;
   if (KIND == K_TRT) hy::trt_fast(f, a.trt, bad);
+  else if (KIND == K_RR) hy::rr_fast(f, a.rr, bad);
   else hy::bgk_fast(f, a.bgk, bad);
   if (bad) {  // outside the hybrid range: the binary64 operator on the same inputs
     hybrid_fallback_cell<KIND>(src, dst, x, y, nx, ny, ld, a.ref);
@@ -187,16 +189,30 @@ hy::TrtParams hybrid_trt_params(const CollParams& cp) {
   return p;
 }
 
+hy::RrParams hybrid_rr_params(const CollParams& cp) {
+  hy::RrParams p;
+  const double w[3] = {W0, WS, WD};
+  for (int i = 0; i < 3; i++) {
+    p.w[i] = w[i];
+    p.wdf[i] = split_const(w[i]);
+  }
+  p.omb = split_const(1.0 - cp.omega);
+  p.third = split_const(1.0 / 3.0);
+  return p;
+}
+
 cudaError_t step_pull_df64(int kind, const Sweep& s, const CollParams& cp) {
-  if (kind != K_BGK && kind != K_TRT) return cudaErrorNotSupported;
+  if (kind != K_BGK && kind != K_TRT && kind != K_RR) return cudaErrorNotSupported;
   const int ft = (s.ny + kBlock - 1) / kBlock;
   const long long blocks = (long long)ft * s.nx;
   if (blocks <= 0 || blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
   HybridArgs a;
   a.bgk = hybrid_params(cp.omega);
   a.trt = hybrid_trt_params(cp);
+  a.rr = hybrid_rr_params(cp);
   a.ref = cp;
   if (kind == K_TRT) return launch_hybrid<K_TRT>(s, (unsigned)blocks, ft, a);
+  if (kind == K_RR) return launch_hybrid<K_RR>(s, (unsigned)blocks, ft, a);
   return launch_hybrid<K_BGK>(s, (unsigned)blocks, ft, a);
 }
 

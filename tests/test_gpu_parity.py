@@ -88,7 +88,7 @@ def hybrid_flag(reset=1):
     return flag.value
 
 
-@pytest.mark.parametrize("kind", ["bgk", "trt"])
+@pytest.mark.parametrize("kind", ["bgk", "trt", "rr"])
 @pytest.mark.parametrize("nx,ny,steps,omega", [(17, 13, 10, 1.25), (64, 64, 1000, 1.6), (64, 64, 1000, 1.9),
                                                (256, 192, 200, 1.25), (33, 48, 500, 1.8)])
 def test_hybrid_within_1e12(gpu_lib, kind, nx, ny, steps, omega):
@@ -108,7 +108,7 @@ def test_hybrid_within_1e12(gpu_lib, kind, nx, ny, steps, omega):
     g.close()
 
 
-@pytest.mark.parametrize("kind", ["bgk", "trt"])
+@pytest.mark.parametrize("kind", ["bgk", "trt", "rr"])
 @pytest.mark.parametrize("rho0", [5.0, 2.5])
 def test_hybrid_out_of_range_cells_fall_back(gpu_lib, kind, rho0):
     """Cells with populations past the hybrid limits (|f_0| >= 2 at rho0 = 5;
@@ -150,7 +150,7 @@ def test_hybrid_long_horizon_bench_state(gpu_lib):
 
 def test_hybrid_rejects_other_collisions(gpu_lib):
     from plbm import LatticeGrid, PlbmError
-    g = LatticeGrid(16, 16, collision="rr", math="hybrid")
+    g = LatticeGrid(16, 16, collision="bgki", math="hybrid")
     with pytest.raises(PlbmError) as e:
         g.perform_lbm_step(1)
     assert e.value.code == -4
