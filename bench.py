@@ -49,7 +49,8 @@ BYTES_PER_CELL = {"f64": 144, "f32dev": 72, "f16dev": 36}
 # DRAM bytes per cell update measured by ncu (dram__bytes_read.sum +
 # dram__bytes_write.sum of one launch / cells) on a 2048^2 capture of the same
 # kernel, scaled by the cell count: profiles/k_step_*_2048_fullset.md.
-NCU_TRAFFIC_PER_CELL = {("f64", "bgk", "hybrid"): 132.7, ("f64", "bgk", "fma"): 132.4}
+NCU_TRAFFIC_PER_CELL = {("f64", "bgk", "hybrid"): 132.6, ("f64", "trt", "hybrid"): 132.9,
+                        ("f64", "rr", "hybrid"): 133.1, ("f64", "bgk", "fma"): 132.4}
 FALLBACK_HBM_GBS = 6800.0
 
 
@@ -318,7 +319,7 @@ def main() -> None:
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.math is None:
-        args.math = "hybrid" if (args.storage == "f64" and args.kind == "bgk") else "fma"
+        args.math = "hybrid" if args.storage == "f64" else "fma"
 
     if args.impl == "reference":
         run_reference(args)
@@ -447,6 +448,13 @@ def main() -> None:
         var = {}
         var["fp64_native"] = variant_entry(n, "f64", time_grid_steps(torch, n, "f64", args.kind, "fma", omega, 20, 3,
                                                                     fields), peak)
+        for other in ("bgk", "trt", "rr"):
+            if other == args.kind:
+                continue
+            for mm in ("hybrid", "fma"):
+                e = variant_entry(n, "f64", time_grid_steps(torch, n, "f64", other, mm, omega, 20, 3, fields), peak)
+                e["workload"] = f"{n}^2 {other.upper()} binary64, {mm} arithmetic, same state and tau"
+                var[f"fp64_{other}_{mm}"] = e
         var["fp32dev"] = variant_entry(n, "f32dev", time_grid_steps(torch, n, "f32dev", args.kind, "fma", omega, 50, 3,
                                                                    fields), peak)
         if args.kind == "bgk":
