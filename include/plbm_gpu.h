@@ -81,9 +81,15 @@ int plbm_grid_info(const plbm_grid_t *g, int *nx, int *ny, int *ld, int *nf, int
 /* grid%iold / grid%inew (1-based). */
 int plbm_grid_indices(const plbm_grid_t *g, int *iold, int *inew);
 int plbm_grid_set_indices(plbm_grid_t *g, int iold, int inew);
+/* grid%iold / grid%inew / grid%imid (imid = 3 when nf > 2, else -1;
+ * src/fvm_bardow.F90:172-177). */
+int plbm_grid_indices3(const plbm_grid_t *g, int *iold, int *inew, int *imid);
+int plbm_grid_set_indices3(plbm_grid_t *g, int iold, int inew, int imid);
 /* Run the handle's work on this cudaStream_t (NULL = the handle's own stream). */
 int plbm_grid_set_stream(plbm_grid_t *g, void *cuda_stream);
-/* Device address of lattice ibuf (for device-resident callers). */
+/* Device address of lattice ibuf (for device-resident callers).  A
+ * plbm_perform_triple_step permutes which device lattice backs which buffer
+ * index: query the address again after one. */
 int plbm_grid_device_ptr(const plbm_grid_t *g, int ibuf, void **dptr);
 
 /* ---- properties --------------------------------------------------------- */
@@ -119,6 +125,14 @@ int plbm_collide(plbm_grid_t *g);
 /* perform_lbm_step -- src/periodic_lbm.f90:15-29, nsteps times: one fused
  * pull-stream + collide kernel per step, then the iold/inew swap. */
 int plbm_perform_lbm_step(plbm_grid_t *g, int nsteps);
+/* perform_triple_step -- src/fvm_bardow.F90:322-340, nsteps times (needs
+ * nf >= 3, PLBM_F64 storage, PLBM_MATH_FMA or _STRICT): stream iold -> inew,
+ * keep the streamed populations in iold, collide inew, rotate
+ * iold <- inew, inew <- imid, imid <- iold.  One fused kernel per step
+ * (read 72 B, write 144 B per cell) writes the pre-collision populations to a
+ * spare lattice (allocated on the first call) that then backs buffer index
+ * iold; every buffer index holds what the Fortran leaves in it. */
+int plbm_perform_triple_step(plbm_grid_t *g, int nsteps);
 /* update_macros -- src/fvm_bardow.F90:343-390: moments of f(:,:,:,inew)
  * into host (ny,nx) arrays.  Any of rho/ux/uy may be NULL. */
 int plbm_update_macros(plbm_grid_t *g, double *rho, double *ux, double *uy);
@@ -163,6 +177,27 @@ int plbm_velocity_l2_error(plbm_grid_t *g, int ibuf, const double *uxa, const do
 int plbm_velocity_l2_error_noalloc(int storage, int nx, int ny, int ld, const void *f,
                                    const double *uxa, const double *uya, double *err,
                                    void *cuda_stream);
+
+/* ---- files (.npy, NumPy format version 1.0) -------------------------------
+ * output_npy -- src/fvm_bardow.F90:930-961, src/output/npy.f90:13-26: the
+ * moments mf(ny,nx,3) = (rho, ux, uy) of f(:,:,:,inew) (as update_macros
+ * computes them) written as a Fortran-order binary64 array of shape
+ * (ny, nx, 3). */
+int plbm_output_npy(plbm_grid_t *g, const char *path);
+/* The same under the reference's name: folder/filename + step as %09d +
+ * ".npy" (step < 0: no number), creating folder (mkdir -p) first. */
+int plbm_output_npy_step(plbm_grid_t *g, const char *folder, const char *filename, int step);
+/* Restart files: all nf lattices as binary64 f(ld,nx,0:8,nf), Fortran order
+ * (deviation storage is converted).  load_state needs the same ld, nx, nf.
+ * Buffer indices are not stored (plbm_grid_indices3 / set_indices3). */
+int plbm_save_state(plbm_grid_t *g, const char *path);
+int plbm_load_state(plbm_grid_t *g, const char *path);
+/* Host-only helpers (no device): write a binary64 array as .npy; read the
+ * header of one (shape has room for 8 extents). */
+int plbm_write_npy(const char *path, const double *data, int ndim, const long long *shape,
+                   int fortran_order);
+int plbm_read_npy_header(const char *path, int *ndim, long long *shape, int *fortran_order,
+                         long long *data_offset);
 
 /* Wait for all work queued on the handle's stream. */
 int plbm_synchronize(plbm_grid_t *g);

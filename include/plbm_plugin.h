@@ -51,6 +51,10 @@ int c_plbmgpu_status(void *sim);
 /* Not in the reference: run nsteps steps in one call (same result as nsteps
  * calls of c_plbmgpu_step). */
 int c_plbmgpu_steps(void *sim, double omega, int nsteps);
+/* Not in the reference: wait until the queued steps have finished (steps run
+ * asynchronously on the instance's stream; vars() waits by itself).  Returns
+ * the sticky status. */
+int c_plbmgpu_synchronize(void *sim);
 
 #ifdef __cplusplus
 }

@@ -141,6 +141,21 @@ def perform_lbm_step(f2: np.ndarray, ny: int, iold: int, inew: int, kind: int, o
     return a.value, b.value
 
 
+def perform_triple_step(f: np.ndarray, ny: int, iold: int, inew: int, imid: int, kind: int, omega: float,
+                        trt_magic: float, nsteps: int):
+    """perform_triple_step x nsteps (src/fvm_bardow.F90:322-340) with lbm_stream as
+    grid%streaming, on f (nf, 9, nx, ld): stream iold -> inew (rows 1:ny,
+    src/periodic_lbm.f90:45-127), f(iold) = f(inew), collide inew in place,
+    then iold <- inew, inew <- imid, imid <- iold.  Returns (iold, inew, imid)."""
+    for _ in range(nsteps):
+        streamed = lbm_stream(f[iold - 1], ny)
+        f[inew - 1][:, :, :ny] = streamed[:, :, :ny]
+        f[iold - 1][...] = f[inew - 1]
+        collide(f[inew - 1], ny, kind, omega, trt_magic)
+        iold, inew, imid = inew, imid, iold
+    return iold, inew, imid
+
+
 def set_properties(nu: float, dt: float, magic: float | None = None):
     t, o, m = C.c_double(), C.c_double(), C.c_double()
     mp = None

@@ -34,6 +34,7 @@ UNITS = [
     ("batched.cu", "batched.o", ["--fmad=true"]),
     ("adjoint.cu", "adjoint.o", ["--fmad=true"]),
     ("grid.cpp", "grid.o", ["-x", "cu", "--fmad=false"]),
+    ("grid_io.cpp", "grid_io.o", ["-x", "cu", "--fmad=false"]),
     ("plugin.cpp", "plugin.o", ["-x", "cu", "--fmad=false"]),
     ("batch.cpp", "batch.o", ["-x", "cu", "--fmad=false"]),
     ("adjoint.cpp", "adjoint_host.o", ["-x", "cu", "--fmad=false"]),

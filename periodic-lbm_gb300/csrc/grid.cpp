@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "../../include/plbm_gpu.h"
+#include "grid_internal.h"
 #include "plbm_launch.h"
 
 using namespace plbm;
@@ -42,74 +43,13 @@ int cuda_fail(cudaError_t e, const char* what) {
                                                   : PLBM_E_CUDA;
   return fail(code, "%s: %s (%s)", what, cudaGetErrorString(e), cudaGetErrorName(e));
 }
-int ok() { return PLBM_OK; }
 }  // namespace plbm_internal
 using namespace plbm_internal;
 
-#define CUDA_TRY(expr, what)                \
-  do {                                      \
-    cudaError_t e_ = (expr);                \
-    if (e_ != cudaSuccess) return cuda_fail(e_, what); \
-  } while (0)
+#define CUDA_TRY(expr, what) PLBM_CUDA_TRY(expr, what)
 
 extern "C" const char* plbm_last_error(void) { return g_last_error.c_str(); }
-extern "C" int plbm_version(void) { return 1 * 10000 + 0 * 100 + 0; }
-
-// ---------------------------------------------------------------------------
-struct plbm_grid {
-  int nx, ny, ld, nf, storage;
-  int kind = PLBM_BGK, math = PLBM_MATH_FMA;
-  int iold = 2, inew = 1;
-  double nu = 0, dt = 1, tau = 0, omega = 1, trt_magic = 0.25;
-  int device = 0;
-  void* f = nullptr;           // nf lattices, contiguous
-  size_t lat_elems = 0;        // ld*nx*9
-  size_t elem_bytes = 8;
-  cudaStream_t own = nullptr;  // stream created by the handle
-  cudaStream_t stream = nullptr;
-  double* scratch = nullptr;   // 3*nx*ny doubles + reduction partials
-  size_t scratch_elems = 0;
-};
-
-namespace {
-
-int pad16(int n) {
-  int r = n % 16;
-  return r > 0 ? n + (16 - r) : n;
-}
-
-int check_grid(const plbm_grid_t* g) {
-  if (!g) return fail(PLBM_E_INVALID, "NULL grid handle");
-  return PLBM_OK;
-}
-
-int check_buf(const plbm_grid_t* g, int ibuf) {
-  if (ibuf < 1 || ibuf > g->nf) return fail(PLBM_E_INVALID, "buffer index %d outside 1..%d", ibuf, g->nf);
-  return PLBM_OK;
-}
-
-void* lattice(const plbm_grid_t* g, int ibuf) {
-  return static_cast<char*>(g->f) + (size_t)(ibuf - 1) * g->lat_elems * g->elem_bytes;
-}
-
-int use_device(const plbm_grid_t* g) {
-  CUDA_TRY(cudaSetDevice(g->device), "cudaSetDevice");
-  return PLBM_OK;
-}
-
-int ensure_scratch(plbm_grid_t* g, size_t elems) {
-  if (g->scratch_elems >= elems) return PLBM_OK;
-  if (g->scratch) cudaFree(g->scratch);
-  g->scratch = nullptr;
-  g->scratch_elems = 0;
-  CUDA_TRY(cudaMalloc(&g->scratch, elems * sizeof(double)), "cudaMalloc(scratch)");
-  g->scratch_elems = elems;
-  return PLBM_OK;
-}
-
-int internal_storage(int storage) { return storage; }  // PLBM_F64/F32DEV/F16DEV == ST_*
-
-}  // namespace
+extern "C" int plbm_version(void) { return 1 * 10000 + 1 * 100 + 0; }
 
 // Relaxation parameters of one launch, as the Fortran forms them:
 //   BGK  omegabar = 1 - omega                      (src/collision_bgk.F90:26)
@@ -169,6 +109,7 @@ extern "C" int plbm_grid_create(int nx, int ny, int nf, int storage, plbm_grid_t
     return cuda_fail(e, "grid setup");
   }
   g->stream = g->own;
+  g->imid = nf > 2 ? 3 : -1;  // src/fvm_bardow.F90:172-177
   *out = g;
   return ok();
 }
@@ -178,6 +119,7 @@ extern "C" int plbm_grid_destroy(plbm_grid_t* g) {
   cudaSetDevice(g->device);
   cudaStreamSynchronize(g->stream);
   if (g->f) cudaFree(g->f);
+  if (g->spare) cudaFree(g->spare);
   if (g->scratch) cudaFree(g->scratch);
   if (g->own) cudaStreamDestroy(g->own);
   delete g;
@@ -208,6 +150,29 @@ extern "C" int plbm_grid_set_indices(plbm_grid_t* g, int iold, int inew) {
   if (iold == inew) return fail(PLBM_E_INVALID, "iold and inew must differ");
   g->iold = iold;
   g->inew = inew;
+  return PLBM_OK;
+}
+
+extern "C" int plbm_grid_indices3(const plbm_grid_t* g, int* iold, int* inew, int* imid) {
+  if (int r = check_grid(g)) return r;
+  if (iold) *iold = g->iold;
+  if (inew) *inew = g->inew;
+  if (imid) *imid = g->imid;
+  return PLBM_OK;
+}
+
+extern "C" int plbm_grid_set_indices3(plbm_grid_t* g, int iold, int inew, int imid) {
+  if (int r = check_grid(g)) return r;
+  if (int r = check_buf(g, iold)) return r;
+  if (int r = check_buf(g, inew)) return r;
+  if (imid != -1) {
+    if (int r = check_buf(g, imid)) return r;
+    if (imid == iold || imid == inew) return fail(PLBM_E_INVALID, "imid must differ from iold and inew");
+  }
+  if (iold == inew) return fail(PLBM_E_INVALID, "iold and inew must differ");
+  g->iold = iold;
+  g->inew = inew;
+  g->imid = imid;
   return PLBM_OK;
 }
 
@@ -404,6 +369,54 @@ extern "C" int plbm_perform_lbm_step(plbm_grid_t* g, int nsteps) {
     const int t = g->iold;  // src/periodic_lbm.f90:22-27
     g->iold = g->inew;
     g->inew = t;
+  }
+  return ok();
+}
+
+// perform_triple_step (src/fvm_bardow.F90:322-340): stream iold -> inew, keep
+// the streamed populations in iold, collide inew in place, then rotate
+// iold <- inew, inew <- imid, imid <- iold.  Done as one fused kernel that
+// writes the pre-collision populations to a spare lattice; the spare then
+// takes the place of buffer iold (the buffer-index -> lattice map is
+// permuted), so every buffer index holds what the Fortran leaves in it.
+extern "C" int plbm_perform_triple_step(plbm_grid_t* g, int nsteps) {
+  if (int r = check_grid(g)) return r;
+  if (nsteps < 0) return fail(PLBM_E_INVALID, "nsteps = %d < 0", nsteps);
+  if (g->imid < 1) return fail(PLBM_E_INVALID, "perform_triple_step needs a third buffer (alloc_grid with nf >= 3)");
+  if (g->storage != PLBM_F64)
+    return fail(PLBM_E_UNSUPPORTED, "perform_triple_step is offered for PLBM_F64 storage");
+  if (g->math != PLBM_MATH_FMA && g->math != PLBM_MATH_STRICT)
+    return fail(PLBM_E_UNSUPPORTED, "perform_triple_step runs with PLBM_MATH_FMA or PLBM_MATH_STRICT");
+  if (int r = use_device(g)) return r;
+  if (!g->spare) {
+    CUDA_TRY(cudaMalloc(&g->spare, g->lat_elems * g->elem_bytes), "cudaMalloc(spare lattice)");
+    CUDA_TRY(cudaMemsetAsync(g->spare, 0, g->lat_elems * g->elem_bytes, g->stream), "clear spare lattice");
+    g->spare_slot = g->nf;
+  }
+  const CollParams p = plbm_make_params(g->omega, g->trt_magic);
+  const bool strict_math = g->math == PLBM_MATH_STRICT;
+  for (int i = 0; i < nsteps; i++) {
+    void* pre = physical(g, g->spare_slot);
+    Sweep s{g->nx, g->ny, g->ld, lattice(g, g->iold), lattice(g, g->inew), g->stream};
+    cudaError_t e;
+    if (g->kind == PLBM_BGKI && g->ld != g->ny) {
+      // the (ny,nx,0:8) dummy of collide_bgk_improved: the reference's passes
+      e = fma::stream_f64(s);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(pre, s.dst, g->lat_elems * g->elem_bytes, cudaMemcpyDeviceToDevice, g->stream);
+      if (e == cudaSuccess) e = strict_math ? strict::collide_f64(g->kind, s, p) : fma::collide_f64(g->kind, s, p);
+    } else {
+      e = strict_math ? strict::step_pull_pre_f64(g->kind, s, pre, p) : fma::step_pull_pre_f64(g->kind, s, pre, p);
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "triple-step kernel");
+    // the spare now holds f(:,:,:,iold) of the Fortran; the old iold lattice is free
+    const int freed = g->slot[g->iold - 1];
+    g->slot[g->iold - 1] = g->spare_slot;
+    g->spare_slot = freed;
+    const int t = g->iold;  // src/fvm_bardow.F90:333-338
+    g->iold = g->inew;
+    g->inew = g->imid;
+    g->imid = t;
   }
   return ok();
 }

@@ -30,6 +30,8 @@ constexpr int kBlock = 256;
   cudaError_t collide_f64(int kind, const Sweep& s, const CollParams& p);                 \
   /* plugin step: shifted binary64 collide + push (sim/sim.F90:404-505), XFast */          \
   cudaError_t step_push_shift_f64(int kind, const Sweep& s, const CollParams& p);         \
+  /* perform_triple_step fused: also stores the pre-collision populations to pre */       \
+  cudaError_t step_pull_pre_f64(int kind, const Sweep& s, void* pre, const CollParams& p); \
   }
 PLBM_DECLARE_F64(fma)
 PLBM_DECLARE_F64(strict)

@@ -213,6 +213,16 @@ extern "C" void c_plbmgpu_free(void* p) {
   if (s) destroy(s);
 }
 
+extern "C" int c_plbmgpu_synchronize(void* p) {
+  PluginSim* s = as_sim(p);
+  if (!s) return fail(PLBM_E_INVALID, "invalid plugin handle");
+  if (s->status) return s->status;
+  cudaError_t e = cudaSetDevice(s->device);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+  if (e != cudaSuccess) s->status = cuda_fail(e, "plugin synchronize");
+  return s->status;
+}
+
 extern "C" int c_plbmgpu_status(void* p) {
   PluginSim* s = as_sim(p);
   if (!s) return fail(PLBM_E_INVALID, "invalid plugin handle");

@@ -12,6 +12,8 @@
 //   k_stream              lbm_stream alone (src/periodic_lbm.f90:45-127).
 //   k_collide             collide_* alone, in place (src/collision_*.F90).
 //   k_collide_bgki_seq    collide_bgk_improved on its (ny,nx,0:8) dummy view.
+//   k_step_pre            perform_triple_step: fused step that also stores the
+//                         pre-collision populations.
 //   k_step<XFast, push>   the plugin step of sim/sim.F90:404-505 + :568-624:
 //                         shifted populations, collide, then push along c_i.
 #include "plbm_launch.h"
@@ -64,6 +66,28 @@ __global__ void __launch_bounds__(kBlock) k_step(const double* __restrict__ src,
     const int dy = PUSH ? wrap_add(y, cy_of(q), ny) : y;
     dst[L::off(dx, dy, q, nx, ny, ld)] = f[q];
   }
+}
+
+// perform_triple_step fused (src/fvm_bardow.F90:322-340): pull-stream from
+// src, store the streamed (pre-collision) populations to pre, collide, store
+// the result to dst.  Reads 72 B and writes 144 B per cell; the reference's
+// three passes (stream, copy, collide) move 432 B.
+template <int KIND>
+__global__ void __launch_bounds__(kBlock) k_step_pre(const double* __restrict__ src, double* __restrict__ pre,
+                                                    double* __restrict__ dst, int nx, int ny, int ld, int ftiles,
+                                                    CollParams p) {
+  int x, y;
+  if (!cell_of<YFast>(ftiles, nx, ny, x, y)) return;
+  double f[9];
+#pragma unroll
+  for (int q = 0; q < 9; q++) {
+    const int sx = wrap_add(x, -cx_of(q), nx), sy = wrap_add(y, -cy_of(q), ny);
+    f[q] = __ldg(src + YFast::off(sx, sy, q, nx, ny, ld));
+    pre[YFast::off(x, y, q, nx, ny, ld)] = f[q];
+  }
+  collide_ref<KIND>(f, p);
+#pragma unroll
+  for (int q = 0; q < 9; q++) dst[YFast::off(x, y, q, nx, ny, ld)] = f[q];
 }
 
 // lbm_stream: fdst(y,x,q) = fsrc(y - cy, x - cx, q) for rows 1:ny.
@@ -137,6 +161,24 @@ cudaError_t step_pull_f64(int kind, const Sweep& s, const CollParams& p) {
 
 cudaError_t step_push_shift_f64(int kind, const Sweep& s, const CollParams& p) {
   return launch_step<XFast, true, true>(kind, s, p);
+}
+
+cudaError_t step_pull_pre_f64(int kind, const Sweep& s, void* pre, const CollParams& p) {
+  const int ft = tiles(s.ny);
+  const long long blocks = (long long)ft * s.nx;
+  if (blocks <= 0 || blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+  const double* a = static_cast<const double*>(s.src);
+  double* b = static_cast<double*>(s.dst);
+  double* c = static_cast<double*>(pre);
+  const unsigned nb = (unsigned)blocks;
+  switch (kind) {
+    case K_BGK: k_step_pre<K_BGK><<<nb, kBlock, 0, s.stream>>>(a, c, b, s.nx, s.ny, s.ld, ft, p); break;
+    case K_TRT: k_step_pre<K_TRT><<<nb, kBlock, 0, s.stream>>>(a, c, b, s.nx, s.ny, s.ld, ft, p); break;
+    case K_RR: k_step_pre<K_RR><<<nb, kBlock, 0, s.stream>>>(a, c, b, s.nx, s.ny, s.ld, ft, p); break;
+    case K_BGKI: k_step_pre<K_BGKI><<<nb, kBlock, 0, s.stream>>>(a, c, b, s.nx, s.ny, s.ld, ft, p); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
 }
 
 cudaError_t stream_f64(const Sweep& s) {

@@ -65,6 +65,15 @@ SIGNATURES = {
     "plbm_grid_info": (C.c_int, [_vp, _ip, _ip, _ip, _ip, _ip]),
     "plbm_grid_indices": (C.c_int, [_vp, _ip, _ip]),
     "plbm_grid_set_indices": (C.c_int, [_vp, C.c_int, C.c_int]),
+    "plbm_grid_indices3": (C.c_int, [_vp, _ip, _ip, _ip]),
+    "plbm_grid_set_indices3": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int]),
+    "plbm_perform_triple_step": (C.c_int, [_vp, C.c_int]),
+    "plbm_output_npy": (C.c_int, [_vp, C.c_char_p]),
+    "plbm_output_npy_step": (C.c_int, [_vp, C.c_char_p, C.c_char_p, C.c_int]),
+    "plbm_save_state": (C.c_int, [_vp, C.c_char_p]),
+    "plbm_load_state": (C.c_int, [_vp, C.c_char_p]),
+    "plbm_write_npy": (C.c_int, [C.c_char_p, _vp, C.c_int, _vp, C.c_int]),
+    "plbm_read_npy_header": (C.c_int, [C.c_char_p, _ip, _vp, _ip, C.POINTER(C.c_longlong)]),
     "plbm_grid_set_stream": (C.c_int, [_vp, _vp]),
     "plbm_grid_device_ptr": (C.c_int, [_vp, C.c_int, C.POINTER(_vp)]),
     "plbm_set_properties": (C.c_int, [_vp, C.c_double, C.c_double, _dp]),
@@ -121,6 +130,7 @@ SIGNATURES = {
     "c_plbmgpu_norm": (C.c_double, [C.c_int, C.c_int, _vp, _vp]),
     "c_plbmgpu_status": (C.c_int, [_vp]),
     "c_plbmgpu_steps": (C.c_int, [_vp, C.c_double, C.c_int]),
+    "c_plbmgpu_synchronize": (C.c_int, [_vp]),
 }
 
 # Entry points added after the first release; bound when the library has them.

@@ -140,6 +140,21 @@ class LatticeGrid:
     def inew(self) -> int:
         return self.indices[1]
 
+    @property
+    def indices3(self) -> tuple[int, int, int]:
+        """(iold, inew, imid), 1-based; imid = -1 for a two-lattice grid."""
+        a, b, c = C.c_int(), C.c_int(), C.c_int()
+        check(self._lib.plbm_grid_indices3(self.handle, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, c.value
+
+    @indices3.setter
+    def indices3(self, v) -> None:
+        check(self._lib.plbm_grid_set_indices3(self.handle, int(v[0]), int(v[1]), int(v[2])))
+
+    @property
+    def imid(self) -> int:
+        return self.indices3[2]
+
     def set_stream(self, stream) -> None:
         """Queue the handle's work on a torch stream or raw cudaStream_t; None = own stream.
 
@@ -189,6 +204,29 @@ class LatticeGrid:
         """perform_lbm_step, nsteps times (fused stream+collide, then swap)."""
         check(self._lib.plbm_perform_lbm_step(self.handle, int(nsteps)))
 
+    def perform_triple_step(self, nsteps: int = 1) -> None:
+        """perform_triple_step (src/fvm_bardow.F90:322-340), nsteps times; nf >= 3."""
+        check(self._lib.plbm_perform_triple_step(self.handle, int(nsteps)))
+
+    # -- files ----------------------------------------------------------------------
+    def output_npy(self, path) -> None:
+        """output_npy: mf(ny,nx,3) of f(:,:,:,inew) as a Fortran-order .npy of shape (ny, nx, 3)."""
+        check(self._lib.plbm_output_npy(self.handle, str(path).encode()))
+
+    def output_npy_step(self, folder, filename: str, step: int = -1) -> str:
+        """The reference's file name: folder/filename + %09d step + .npy (folder created)."""
+        check(self._lib.plbm_output_npy_step(self.handle, str(folder).encode() if folder else None,
+                                             filename.encode(), int(step)))
+        name = filename + (f"{step:09d}" if step >= 0 else "") + ".npy"
+        return f"{folder}/{name}" if folder else f"/{name}"
+
+    def save_state(self, path) -> None:
+        """All nf lattices as a Fortran-order binary64 .npy of shape (ld, nx, 9, nf)."""
+        check(self._lib.plbm_save_state(self.handle, str(path).encode()))
+
+    def load_state(self, path) -> None:
+        check(self._lib.plbm_load_state(self.handle, str(path).encode()))
+
     def update_macros(self) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
         """update_macros: moments of f(:,:,:,inew) as (nx, ny) arrays."""
         shp = (self.nx, self.ny)
@@ -227,3 +265,26 @@ def vorticity(ux, uy, order: int = 2) -> np.ndarray:
     w = np.empty_like(ux)
     check(lib.plbm_vorticity(int(order), nx, ny, ptr(ux), ptr(uy), ptr(w)))
     return w
+
+
+def write_npy(path, a: np.ndarray, fortran_order: bool = True) -> None:
+    """Write a float64 array with the library's .npy writer (host only).
+
+    fortran_order=True writes a's Fortran-order data (numpy reads back ``a``)."""
+    arr = np.asarray(a, dtype=np.float64)
+    data = np.asfortranarray(arr) if fortran_order else np.ascontiguousarray(arr)
+    shape = (C.c_longlong * max(arr.ndim, 1))(*arr.shape)
+    buf = data.ravel(order="F" if fortran_order else "C")
+    check(_lib.load().plbm_write_npy(str(path).encode(), ptr(buf), arr.ndim, C.cast(shape, C.c_void_p),
+                                     int(bool(fortran_order))))
+
+
+def read_npy_header(path) -> dict:
+    """Header of a .npy file as the library parses it."""
+    nd, fo, off = C.c_int(), C.c_int(), C.c_longlong()
+    shape = (C.c_longlong * 8)()
+    check(_lib.load().plbm_read_npy_header(str(path).encode(), C.byref(nd), C.cast(shape, C.c_void_p),
+                                           C.byref(fo), C.byref(off)))
+    return {"shape": tuple(shape[i] for i in range(nd.value)), "fortran_order": bool(fo.value),
+            "data_offset": off.value}
+

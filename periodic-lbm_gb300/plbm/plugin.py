@@ -67,6 +67,10 @@ class SimPlugin:
         if self._status is not None:
             self._status.restype = ctypes.c_int
             self._status.argtypes = (ctypes.c_void_p,)
+        self._sync = getattr(self.lib, "c_" + name + "_synchronize", None)
+        if self._sync is not None:
+            self._sync.restype = ctypes.c_int
+            self._sync.argtypes = (ctypes.c_void_p,)
         self._steps = getattr(self.lib, "c_" + name + "_steps", None)
         if self._steps is not None:
             self._steps.restype = ctypes.c_int
@@ -123,6 +127,12 @@ class SimPlugin:
                 self.step(omega)
         else:
             _lib.check(self._steps(self.ptr, ctypes.c_double(omega), int(nsteps)))
+
+    def synchronize(self):
+        """Wait for queued steps (a no-op for plugins without the entry point,
+        whose steps are synchronous)."""
+        if self._sync is not None and self.ptr is not None:
+            _lib.check(self._sync(self.ptr))
 
     def _check(self):
         if self._status is not None and self.ptr is not None:

@@ -326,3 +326,76 @@ def test_errors_are_reported(gpu_lib):
     assert e.value.code == -4
     g.close()
     d.close()
+
+
+@pytest.mark.parametrize("kind,omega", [("bgk", 1.25), ("trt", 1.6), ("rr", 1.9), ("bgki", 1.3)])
+@pytest.mark.parametrize("nx,ny,nf", [(17, 13, 3), (24, 32, 3), (20, 16, 4)])
+def test_triple_step_strict_bit_identical(gpu_lib, kind, omega, nx, ny, nf):
+    """perform_triple_step (src/fvm_bardow.F90:322-340): every buffer index holds
+    what the Fortran leaves in it, and the indices rotate the same way."""
+    from plbm import LatticeGrid
+    f0 = initial_state(nx, ny, u0=0.02)
+    ld = f0.shape[-1]
+    rng = np.random.default_rng(3)
+    bufs = [rng.standard_normal((9, nx, ld)) * 0.01 + 0.1 for _ in range(nf)]
+    bufs[1] = f0.copy()  # iold = 2
+    ref = np.stack([b.copy() for b in bufs])
+    g = LatticeGrid(nx, ny, nf=nf, collision=kind, math="strict")
+    g.set_relaxation(omega, 0.25)
+    for b in range(nf):
+        g.upload(bufs[b], b + 1)
+    assert g.indices3 == (2, 1, 3)
+    steps = 5
+    idx = O.perform_triple_step(ref, ny, 2, 1, 3, KIND[kind], omega, 0.25, steps)
+    g.perform_triple_step(steps)
+    assert g.indices3 == idx
+    for b in range(nf):
+        assert np.array_equal(g.download(b + 1)[:, :, :ny], ref[b][:, :, :ny]), b
+    # update_macros reads f(:,:,:,inew) after the rotation
+    for a, c in zip(g.update_macros(), O.update_macros(ref[idx[1] - 1], ny)):
+        assert np.array_equal(a, c)
+    g.close()
+
+
+def test_triple_step_fma_and_plain_steps_interleave(gpu_lib):
+    """FMA build within 1e-12 of the oracle, with perform_lbm_step calls between
+    triple steps (both use the same buffer-index map)."""
+    from plbm import LatticeGrid
+    nx, ny = 40, 24
+    f0 = initial_state(nx, ny)
+    ref = np.zeros((3, 9, nx, f0.shape[-1]))
+    ref[1] = f0
+    g = LatticeGrid(nx, ny, nf=3, collision="trt")
+    g.set_relaxation(1.4, 0.25)
+    g.upload(f0, 2)
+    idx = O.perform_triple_step(ref, ny, 2, 1, 3, O.TRT, 1.4, 0.25, 3)
+    g.perform_triple_step(3)
+    two = np.stack([ref[idx[1] - 1], ref[idx[0] - 1]])  # (inew, iold) as buffers 1, 2
+    io, inew = O.perform_lbm_step(two, ny, 2, 1, O.TRT, 1.4, 0.25, 4)
+    g.perform_lbm_step(4)
+    got = g.download(g.iold)
+    want = two[io - 1]
+    assert relinf(got[:, :, :ny], want[:, :, :ny]) <= TOL
+    g.close()
+
+
+def test_triple_step_errors(gpu_lib):
+    from plbm import LatticeGrid, PlbmError
+    g = LatticeGrid(8, 8)  # nf = 2: no imid
+    assert g.indices3 == (2, 1, -1)
+    with pytest.raises(PlbmError) as e:
+        g.perform_triple_step(1)
+    assert e.value.code == -1
+    g.close()
+    g = LatticeGrid(8, 8, nf=3, storage="f32dev")
+    with pytest.raises(PlbmError) as e:
+        g.perform_triple_step(1)
+    assert e.value.code == -4
+    g.close()
+    g = LatticeGrid(8, 8, nf=3, math="hybrid")
+    with pytest.raises(PlbmError) as e:
+        g.perform_triple_step(1)
+    assert e.value.code == -4
+    with pytest.raises(PlbmError):
+        g.indices3 = (1, 1, 3)
+    g.close()

@@ -125,3 +125,29 @@ def test_plugin_other_collisions_conserve(gpu_lib, kind):
     assert abs(r1.sum() - r0.sum()) < 1e-10 * r0.sum()
     jx0, jx1 = (r0 * u0[:, :, 0]).sum(), (r1 * u1[:, :, 0]).sum()
     assert abs(jx1 - jx0) < 1e-12
+
+
+def test_studies_convergence_on_gpu_plugin(gpu_lib):
+    """plbm.studies.convergence (sim/cases.py:main) through libplbmgpu.so: the
+    same errors as the oracle's plugin restatement, second order, and the L2
+    errors listed beside the reference study (sim/cases.py:357-365) to 1.5 %."""
+    import sys
+    from pathlib import Path
+    sys.path.insert(0, str(Path(__file__).parent))
+    from test_studies import OraclePlugin
+    from plbm import studies
+    from plbm.plugin import SimPlugin
+    gpu = studies.convergence(SimPlugin(), None, base=10, nref=4)
+    cpu = studies.convergence(OraclePlugin(), None, base=10, nref=4)
+    for a, b in zip(gpu["levels"], cpu["levels"]):
+        assert abs(a["l2"] - b["l2"]) <= 1e-9 * b["l2"]
+        assert abs(a["l2"] / studies.REFERENCE_FERR[a["n"]] - 1.0) < 0.015
+    for r in gpu["ratios"]:
+        assert 3.9 < r["l2"] < 4.1
+
+
+def test_studies_perfsweep_on_gpu_plugin(gpu_lib):
+    from plbm import studies
+    from plbm.plugin import SimPlugin
+    out = studies.perfsweep(SimPlugin(), 256, 1024, step=256, tsteps=50, dt=1.0)
+    assert out["grids"] == [256, 512, 768] and min(out["mlups"]) > 0
