@@ -9,7 +9,10 @@
 !>   collide_rr_gpu(grid)       collision_interface, src/collision_regularized.F90:21
 !>   collide_bgk_improved_gpu(grid)  src/collision_bgk_improved.f90:16
 !>   perform_lbm_step_gpu(grid) src/periodic_lbm.f90:15-29, one fused kernel
+!>   perform_triple_step_gpu(grid)  src/fvm_bardow.F90:322-340, one fused kernel
 !>   update_macros_gpu(grid)    src/fvm_bardow.F90:343-390
+!>   output_npy_gpu(grid[,step])  src/fvm_bardow.F90:930-961, moments of the
+!>                              device state written as .npy
 !>
 !> The lattice lives on the device between calls; grid%f on the host is only
 !> read by plbm_gpu_attach / plbm_gpu_upload and written by plbm_gpu_download.
@@ -27,7 +30,7 @@
 module plbm_gpu
 
    use, intrinsic :: iso_c_binding, only: c_int, c_double, c_ptr, c_null_ptr, c_loc, &
-      c_associated, c_char, c_f_pointer, c_intptr_t
+      c_associated, c_char, c_f_pointer, c_intptr_t, c_null_char
    use precision, only: wp
    use fvm_bardow, only: lattice_grid
 
@@ -36,6 +39,7 @@ module plbm_gpu
 
    public :: plbm_gpu_attach, plbm_gpu_detach, plbm_gpu_upload, plbm_gpu_download
    public :: lbm_stream_gpu, perform_lbm_step_gpu, update_macros_gpu
+   public :: perform_triple_step_gpu, output_npy_gpu
    public :: collide_bgk_gpu, collide_trt_gpu, collide_rr_gpu, collide_bgk_improved_gpu
    public :: PLBM_MATH_FMA, PLBM_MATH_STRICT, PLBM_MATH_HYBRID
 
@@ -105,6 +109,22 @@ module plbm_gpu
       end function
       type(c_ptr) function plbm_last_error() bind(c, name="plbm_last_error")
          import :: c_ptr
+      end function
+      integer(c_int) function plbm_grid_set_indices3(g, iold, inew, imid) bind(c, name="plbm_grid_set_indices3")
+         import :: c_int, c_ptr
+         type(c_ptr), value :: g
+         integer(c_int), value :: iold, inew, imid
+      end function
+      integer(c_int) function plbm_perform_triple_step(g, nsteps) bind(c, name="plbm_perform_triple_step")
+         import :: c_int, c_ptr
+         type(c_ptr), value :: g
+         integer(c_int), value :: nsteps
+      end function
+      integer(c_int) function plbm_output_npy_step(g, folder, filename, step) bind(c, name="plbm_output_npy_step")
+         import :: c_int, c_ptr, c_char
+         type(c_ptr), value :: g
+         character(kind=c_char), intent(in) :: folder(*), filename(*)
+         integer(c_int), value :: step
       end function
    end interface
 
@@ -272,6 +292,45 @@ contains
       itmp = grid%iold
       grid%iold = grid%inew
       grid%inew = itmp
+   end subroutine
+
+   !> perform_triple_step with one fused kernel (the pre-collision populations
+   !> land in f(:,:,:,iold) of the device state, as in the reference); the
+   !> index rotation is the reference's (src/fvm_bardow.F90:333-338).
+   subroutine perform_triple_step_gpu(grid, kind)
+      class(lattice_grid), intent(inout) :: grid
+      integer(c_int), intent(in), optional :: kind
+      type(c_ptr) :: h
+      integer :: itmp
+      integer(c_int) :: k
+      k = PLBM_BGK
+      if (present(kind)) k = kind
+      h = handle_of(grid)
+      call sync_state(grid, h, k)
+      call check(plbm_grid_set_indices3(h, int(grid%iold, c_int), int(grid%inew, c_int), int(grid%imid, c_int)), &
+                 "plbm_grid_set_indices3")
+      call check(plbm_perform_triple_step(h, 1_c_int), "plbm_perform_triple_step")
+      itmp = grid%iold
+      grid%iold = grid%inew
+      grid%inew = grid%imid
+      grid%imid = itmp
+   end subroutine
+
+   !> output_npy: grid%foldername/grid%filename + step (I0.9) + '.npy' holding
+   !> mf(ny,nx,3) of the device state's f(:,:,:,inew).
+   subroutine output_npy_gpu(grid, step)
+      class(lattice_grid), intent(in) :: grid
+      integer, intent(in), optional :: step
+      type(c_ptr) :: h
+      integer(c_int) :: s
+      character(len=:), allocatable :: folder
+      s = -1
+      if (present(step)) s = int(step, c_int)
+      folder = ''
+      if (allocated(grid%foldername)) folder = trim(grid%foldername)
+      h = handle_of(grid)
+      call sync_state(grid, h, -1_c_int)
+      call check(plbm_output_npy_step(h, folder//c_null_char, grid%filename//c_null_char, s), "plbm_output_npy_step")
    end subroutine
 
    !> update_macros: moments of f(:,:,:,inew) into grid%rho, grid%ux, grid%uy.

@@ -82,7 +82,7 @@ def test_autograd_against_central_differences(gpu_lib):
     scale = np.max(np.abs(gu))
     for _ in range(8):
         a, i, j = int(rng.integers(2)), int(rng.integers(nx)), int(rng.integers(ny))
-        h = 1e-4 * max(abs(float(u0[a, i, j])), 1e-3)
+        h = 1e-4 * max(abs(u0[a, i, j].item()), 1e-3)
         up = u0.detach().clone()
         um = u0.detach().clone()
         up[a, i, j] += h
