@@ -64,6 +64,24 @@ extern "C" {
 #define PLBM_MATH_HYBRID 2
 #define PLBM_MATH_DF64   3
 
+/* ---- streaming schemes (grid%streaming => ...) ----------------------------
+ * LBM       lbm_stream, src/periodic_lbm.f90:32-129 (default; fused with the
+ *           collision in plbm_perform_lbm_step)
+ * FVM_BARDOW        stream_fvm_bardow, src/fvm_bardow.F90:393-509
+ * FDM_BARDOW        stream_fdm_bardow, src/fvm_bardow.F90:511-686, central
+ *                   differences (the default build)
+ * FDM_BARDOW_ISO    the same with the isotropic differences (FDM_ISO build)
+ * FDM_BARDOW_WLS    the same with unweighted least squares (FDM_WLS build)
+ * FDM_SOFONEA       stream_fdm_sofonea, src/fvm_bardow.F90:688-886
+ * The finite-volume / finite-difference schemes use grid%dt (set_properties)
+ * and run with PLBM_F64 storage, FMA or STRICT arithmetic. */
+#define PLBM_STREAM_LBM            0
+#define PLBM_STREAM_FVM_BARDOW     1
+#define PLBM_STREAM_FDM_BARDOW     2
+#define PLBM_STREAM_FDM_BARDOW_ISO 3
+#define PLBM_STREAM_FDM_BARDOW_WLS 4
+#define PLBM_STREAM_FDM_SOFONEA    5
+
 typedef struct plbm_grid plbm_grid_t;
 
 /* Message of the last failing call on this thread ("" if none). */
@@ -101,11 +119,17 @@ int plbm_get_properties(const plbm_grid_t *g, double *nu, double *dt, double *ta
                         double *omega, double *trt_magic);
 /* Set omega and the TRT magic parameter directly. */
 int plbm_set_relaxation(plbm_grid_t *g, double omega, double trt_magic);
+/* Set grid%dt alone (the time step of the finite-volume / finite-difference
+ * streaming schemes); omega is left as it is. */
+int plbm_set_time_step(plbm_grid_t *g, double dt);
 /* grid%collision => collide_bgk | collide_trt | collide_rr | collide_bgk_improved
  * (app/main_taylor_green.f90:39). */
 int plbm_set_collision(plbm_grid_t *g, int kind);
 /* PLBM_MATH_* for PLBM_F64 storage. */
 int plbm_set_math(plbm_grid_t *g, int math);
+/* grid%streaming => lbm_stream | stream_fvm_bardow | stream_fdm_bardow |
+ * stream_fdm_sofonea (PLBM_STREAM_*; app/main_vortex.f90:44). */
+int plbm_set_streaming(plbm_grid_t *g, int scheme);
 
 /* ---- transfers ---------------------------------------------------------- */
 /* Copy host f(:,:,:,ibuf) (ld*nx*9 doubles) to/from the device lattice.
@@ -118,12 +142,14 @@ int plbm_download(plbm_grid_t *g, double *f_host, int ibuf);
  * (ny,nx) arrays; writes the equilibrium into f(:,:,:,iold) on the device. */
 int plbm_set_pdf_to_equilibrium(plbm_grid_t *g, const double *rho, const double *ux,
                                 const double *uy);
-/* lbm_stream -- src/periodic_lbm.f90:32-129: f(:,:,:,iold) -> f(:,:,:,inew). */
+/* grid%streaming() -- lbm_stream (src/periodic_lbm.f90:32-129) or the
+ * selected scheme: f(:,:,:,iold) -> f(:,:,:,inew). */
 int plbm_stream(plbm_grid_t *g);
 /* grid%collision() -- in place on f(:,:,:,inew). */
 int plbm_collide(plbm_grid_t *g);
 /* perform_lbm_step -- src/periodic_lbm.f90:15-29, nsteps times: one fused
- * pull-stream + collide kernel per step, then the iold/inew swap. */
+ * pull-stream + collide kernel per step (lbm_stream; another streaming
+ * scheme: its kernel, then the collision), then the iold/inew swap. */
 int plbm_perform_lbm_step(plbm_grid_t *g, int nsteps);
 /* perform_triple_step -- src/fvm_bardow.F90:322-340, nsteps times (needs
  * nf >= 3, PLBM_F64 storage, PLBM_MATH_FMA or _STRICT): stream iold -> inew,

@@ -55,6 +55,10 @@ def lib(fast: bool = False) -> C.CDLL:
             "oref_equilibrium": (None, [d, d, d, vp]),
             "oref_set_pdf_to_equilibrium": (None, [i, i, i, vp, vp, vp, vp]),
             "oref_perform_lbm_step": (None, [i, i, i, vp, vp, vp, i, d, d, i]),
+            "oref_stream_fvm_bardow": (None, [i, i, i, vp, vp, d]),
+            "oref_stream_fdm_bardow": (None, [i, i, i, vp, vp, d, i]),
+            "oref_stream_fdm_sofonea": (None, [i, i, i, vp, vp, d]),
+            "oref_perform_step_scheme": (None, [i, i, i, vp, vp, vp, i, d, i, d, d, i]),
             "oref_taylor_green_eval": (None, [i, i, d, d, d, d, d, vp, vp, vp, i]),
             "oref_shear_layer_eval": (None, [i, i, d, d, d, d, d, vp, vp, vp]),
             "oref_tgv_l2_norm": (d, [i, i, vp, vp, vp, vp]),
@@ -138,6 +142,40 @@ def perform_lbm_step(f2: np.ndarray, ny: int, iold: int, inew: int, kind: int, o
     a, b = C.c_int(iold), C.c_int(inew)
     lib(fast).oref_perform_lbm_step(nx, ny, ld, _p(f2), C.addressof(a), C.addressof(b), kind, omega,
                                     trt_magic, nsteps)
+    return a.value, b.value
+
+
+# streaming schemes of src/fvm_bardow.F90 (grid%streaming)
+SCHEMES = {"lbm": 0, "fvm_bardow": 1, "fdm_bardow": 2, "fdm_bardow_iso": 3, "fdm_bardow_wls": 4,
+           "fdm_sofonea": 5}
+
+
+def stream_scheme(fold: np.ndarray, ny: int, scheme: str, dt: float, fnew: np.ndarray | None = None,
+                  fast: bool = False) -> np.ndarray:
+    """grid%streaming of the named scheme from fold (9, nx, ld) into fnew
+    (src/fvm_bardow.F90:393-886; lbm_stream for "lbm")."""
+    nx, ld = _nx_ld(fold)
+    fnew = np.zeros_like(fold) if fnew is None else fnew
+    L = lib(fast)
+    s = SCHEMES[scheme]
+    if s == 0:
+        L.oref_lbm_stream(nx, ny, ld, _p(fold), _p(fnew))
+    elif s == 1:
+        L.oref_stream_fvm_bardow(nx, ny, ld, _p(fold), _p(fnew), dt)
+    elif s in (2, 3, 4):
+        L.oref_stream_fdm_bardow(nx, ny, ld, _p(fold), _p(fnew), dt, s - 2)
+    else:
+        L.oref_stream_fdm_sofonea(nx, ny, ld, _p(fold), _p(fnew), dt)
+    return fnew
+
+
+def perform_step_scheme(f2: np.ndarray, ny: int, iold: int, inew: int, scheme: str, dt: float, kind: int,
+                        omega: float, trt_magic: float, nsteps: int, fast: bool = False):
+    """perform_lbm_step x nsteps with grid%streaming => the named scheme."""
+    nx, ld = _nx_ld(f2)
+    a, b = C.c_int(iold), C.c_int(inew)
+    lib(fast).oref_perform_step_scheme(nx, ny, ld, _p(f2), C.addressof(a), C.addressof(b), SCHEMES[scheme],
+                                       dt, kind, omega, trt_magic, nsteps)
     return a.value, b.value
 
 

@@ -557,6 +557,157 @@ void oref_perform_lbm_step(int nx, int ny, int ld, double *f, int *iold, int *in
 }
 
 /* ------------------------------------------------------------------------ */
+/* Finite-volume / finite-difference streaming (src/fvm_bardow.F90:393-886).  */
+/* The reference loops x = 1, ny and y = 1, nx in stream_fvm_bardow and      */
+/* stream_fdm_sofonea (:436,444 and :724,727...), which covers the grid only */
+/* when nx == ny; these restatements loop over the whole grid (x = 1, nx,    */
+/* y = 1, ny), identical for square grids.                                   */
+static const double CXD[9] = {0, 1, 0, -1, 0, 1, -1, -1, 1};
+static const double CYD[9] = {0, 0, 1, 0, -1, 1, 1, -1, -1};
+
+/* stream_fvm_bardow, src/fvm_bardow.F90:409-506 (bilinear face values) */
+void oref_stream_fvm_bardow(int nx, int ny, int ld, const double *fold, double *fnew, double dt)
+{
+    const double p2 = 0.5, p8 = 0.125;
+    for (int x = 0; x < nx; x++)
+        for (int y = 0; y < ny; y++) fnew[IDX(y, x, 0)] = fold[IDX(y, x, 0)];
+    for (int q = 1; q <= 8; q++) {
+        const double cxq = dt * CXD[q], cyq = dt * CYD[q];
+#pragma omp parallel for schedule(static)
+        for (int x1 = 1; x1 <= nx; x1++) {
+            const int xp = xp1_of(x1, nx) - 1, xm = xm1_of(x1, nx) - 1, x = x1 - 1;
+            for (int y1 = 1; y1 <= ny; y1++) {
+                const int yp = xp1_of(y1, ny) - 1, ym = xm1_of(y1, ny) - 1, y = y1 - 1;
+                const double fc = fold[IDX(y, x, q)], fe = fold[IDX(y, xp, q)], fn = fold[IDX(yp, x, q)];
+                const double fw = fold[IDX(y, xm, q)], fs = fold[IDX(ym, x, q)];
+                const double fne = fold[IDX(yp, xp, q)], fnw = fold[IDX(yp, xm, q)];
+                const double fsw = fold[IDX(ym, xm, q)], fse = fold[IDX(ym, xp, q)];
+                const double cfw = p2 * (fc + fw) - p2 * cxq * (fc - fw) - p8 * cyq * (fnw + fn - fsw - fs);
+                const double cfn = p2 * (fc + fn) - p2 * cyq * (fn - fc) - p8 * cxq * (fne + fe - fnw - fw);
+                const double cfe = p2 * (fc + fe) - p2 * cxq * (fe - fc) - p8 * cyq * (fne + fn - fse - fs);
+                const double cfs = p2 * (fc + fs) - p2 * cyq * (fc - fs) - p8 * cxq * (fse + fe - fsw - fw);
+                fnew[IDX(y, x, q)] = fc - cxq * (cfe - cfw) - cyq * (cfn - cfs);
+            }
+        }
+    }
+}
+
+/* stream_fdm_bardow, src/fvm_bardow.F90:526-685.  variant 0: central
+ * differences (the default build, :656-663); 1: isotropic differences of
+ * Kumar 2004 (FDM_ISO, :645-655); 2: unweighted least squares (FDM_WLS,
+ * :597-607). */
+void oref_stream_fdm_bardow(int nx, int ny, int ld, const double *fold, double *fnew, double dt, int variant)
+{
+    const double p2 = 0.5;
+    const double two_thirds = 2.0 / 3.0, one_sixth = 1.0 / 6.0;
+    const double five_sixths = 10.0 / 12.0, one_twelth = 1.0 / 12.0, one_third = 1.0 / 3.0;
+    /* :561 fnew(:,:,0) = fold(:,:,0) (all ld rows) */
+    for (int x = 0; x < nx; x++)
+        for (int y = 0; y < ld; y++) fnew[IDX(y, x, 0)] = fold[IDX(y, x, 0)];
+    for (int q = 1; q <= 8; q++) {
+        const double cxq = dt * CXD[q], cyq = dt * CYD[q];
+        const double cxxq = 0.5 * cxq * cxq, cyyq = 0.5 * cyq * cyq, cxyq = cxq * cyq;
+#pragma omp parallel for schedule(static)
+        for (int x1 = 1; x1 <= nx; x1++) {
+            const int xp = xp1_of(x1, nx) - 1, xm = xm1_of(x1, nx) - 1, x = x1 - 1;
+            for (int y1 = 1; y1 <= ny; y1++) {
+                const int yp = xp1_of(y1, ny) - 1, ym = xm1_of(y1, ny) - 1, y = y1 - 1;
+                const double fc = fold[IDX(y, x, q)], fe = fold[IDX(y, xp, q)], fn = fold[IDX(yp, x, q)];
+                const double fw = fold[IDX(y, xm, q)], fs = fold[IDX(ym, x, q)];
+                const double fne = fold[IDX(yp, xp, q)], fnw = fold[IDX(yp, xm, q)];
+                const double fsw = fold[IDX(ym, xm, q)], fse = fold[IDX(ym, xp, q)];
+                double dfx, dfy, dfxx, dfyy, dfxy;
+                if (variant == 1) {
+                    dfx = p2 * (one_sixth * (fne - fnw) + two_thirds * (fe - fw) + one_sixth * (fse - fsw));
+                    dfy = p2 * (one_sixth * (fne - fse) + two_thirds * (fn - fs) + one_sixth * (fnw - fsw));
+                    dfxx = one_twelth * (fne - 2 * fn + fnw) + five_sixths * (fe - 2 * fc + fw) +
+                           one_twelth * (fse - 2 * fs + fsw);
+                    dfyy = one_twelth * (fne - 2 * fe + fse) + five_sixths * (fn - 2 * fc + fs) +
+                           one_twelth * (fnw - 2 * fw + fsw);
+                    dfxy = 0.25 * (fne - fse - fnw + fsw);
+                } else if (variant == 2) {
+                    dfx = one_sixth * ((fne - fnw) + (fe - fw) + (fse - fsw));
+                    dfy = one_sixth * ((fne - fse) + (fn - fs) + (fnw - fsw));
+                    dfxx = one_third * (fne - 2 * fn + fnw) + one_third * (fe - 2 * fc + fw) +
+                           one_third * (fse - 2 * fs + fsw);
+                    dfyy = one_third * (fne - 2 * fe + fse) + one_third * (fn - 2 * fc + fs) +
+                           one_third * (fnw - 2 * fw + fsw);
+                    dfxy = 0.25 * (fne - fnw + fsw - fse);
+                } else {
+                    dfx = p2 * (fe - fw);
+                    dfy = p2 * (fn - fs);
+                    dfxx = fe - 2 * fc + fw;
+                    dfyy = fn - 2 * fc + fs;
+                    dfxy = 0.25 * (fne - fse - fnw + fsw);
+                }
+                fnew[IDX(y, x, q)] = fc - cxq * dfx - cyq * dfy + (cxxq * dfxx + cxyq * dfxy + cyyq * dfyy);
+            }
+        }
+    }
+}
+
+/* stream_fdm_sofonea, src/fvm_bardow.F90:702-884: Lax-Wendroff along each
+ * lattice direction, fu = f(x + c_q), fd = f(x - c_q). */
+void oref_stream_fdm_sofonea(int nx, int ny, int ld, const double *fold, double *fnew, double dt)
+{
+    const double p2 = 0.5 / sqrt(2.0);
+    /* :719 fnew(:,:,0) = fold(:,:,0) (all ld rows) */
+    for (int x = 0; x < nx; x++)
+        for (int y = 0; y < ld; y++) fnew[IDX(y, x, 0)] = fold[IDX(y, x, 0)];
+    for (int q = 1; q <= 8; q++) {
+        const int cxi = (int)CXD[q], cyi = (int)CYD[q];
+#pragma omp parallel for schedule(static)
+        for (int x1 = 1; x1 <= nx; x1++) {
+            const int xp = xp1_of(x1, nx) - 1, xm = xm1_of(x1, nx) - 1, x = x1 - 1;
+            for (int y1 = 1; y1 <= ny; y1++) {
+                const int yp = xp1_of(y1, ny) - 1, ym = xm1_of(y1, ny) - 1, y = y1 - 1;
+                const int xu = cxi > 0 ? xp : (cxi < 0 ? xm : x), xd = cxi > 0 ? xm : (cxi < 0 ? xp : x);
+                const int yu = cyi > 0 ? yp : (cyi < 0 ? ym : y), yd = cyi > 0 ? ym : (cyi < 0 ? yp : y);
+                const double fc = fold[IDX(y, x, q)], fu = fold[IDX(yu, xu, q)], fd = fold[IDX(yd, xd, q)];
+                double du1, du2;
+                if (q <= 4) {
+                    du1 = 0.5 * (fu - fd);
+                    du2 = fu - 2 * fc + fd;
+                } else {
+                    du1 = p2 * (fu - fd);
+                    du2 = 0.5 * (fu - 2 * fc + fd);
+                }
+                fnew[IDX(y, x, q)] = fc + dt * (0.5 * dt * du2 - du1);
+            }
+        }
+    }
+}
+
+/* perform_lbm_step with grid%streaming => stream_* (src/periodic_lbm.f90:15-29):
+ * scheme 0 lbm_stream, 1 stream_fvm_bardow, 2/3/4 stream_fdm_bardow (central,
+ * isotropic, least squares), 5 stream_fdm_sofonea. */
+void oref_perform_step_scheme(int nx, int ny, int ld, double *f, int *iold, int *inew, int scheme, double dt,
+                              int kind, double omega, double trt_magic, int nsteps)
+{
+    size_t lat = (size_t)ld * (size_t)nx * 9u;
+    for (int s = 0; s < nsteps; s++) {
+        double *fo = f + (size_t)(*iold - 1) * lat;
+        double *fn = f + (size_t)(*inew - 1) * lat;
+        switch (scheme) {
+        case 1: oref_stream_fvm_bardow(nx, ny, ld, fo, fn, dt); break;
+        case 2: case 3: case 4: oref_stream_fdm_bardow(nx, ny, ld, fo, fn, dt, scheme - 2); break;
+        case 5: oref_stream_fdm_sofonea(nx, ny, ld, fo, fn, dt); break;
+        default: oref_lbm_stream(nx, ny, ld, fo, fn); break;
+        }
+        switch (kind) {
+        case OREF_BGK: oref_collide_bgk(nx, ny, ld, fn, omega, 0); break;
+        case OREF_TRT: oref_collide_trt(nx, ny, ld, fn, omega, oref_lambda_d(omega, trt_magic), 0); break;
+        case OREF_RR: oref_collide_rr(nx, ny, ld, fn, omega); break;
+        case OREF_BGKI: oref_collide_bgk_improved(nx, ny, fn, omega); break;
+        default: break;
+        }
+        int t = *iold;
+        *iold = *inew;
+        *inew = t;
+    }
+}
+
+/* ------------------------------------------------------------------------ */
 /* src/benchmarks/taylor_green.f90:51-84 (t >= 0); arrays (ny,nx)            */
 void oref_taylor_green_eval(int nx, int ny, double kx, double ky, double umax, double nu,
                             double t, double *p, double *ux, double *uy, int ref_loop)

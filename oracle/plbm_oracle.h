@@ -57,6 +57,14 @@ void oref_set_pdf_to_equilibrium(int nx, int ny, int ld, const double *rho,
 enum { OREF_BGK = 0, OREF_TRT = 1, OREF_RR = 2, OREF_BGKI = 3 };
 void oref_perform_lbm_step(int nx, int ny, int ld, double *f, int *iold, int *inew,
                            int kind, double omega, double trt_magic, int nsteps);
+/* Finite-volume / finite-difference streaming, src/fvm_bardow.F90:393-886
+ * (loops over the whole nx x ny grid; the reference's swapped bounds in
+ * stream_fvm_bardow / stream_fdm_sofonea agree with them for nx == ny). */
+void oref_stream_fvm_bardow(int nx, int ny, int ld, const double *fold, double *fnew, double dt);
+void oref_stream_fdm_bardow(int nx, int ny, int ld, const double *fold, double *fnew, double dt, int variant);
+void oref_stream_fdm_sofonea(int nx, int ny, int ld, const double *fold, double *fnew, double dt);
+void oref_perform_step_scheme(int nx, int ny, int ld, double *f, int *iold, int *inew, int scheme, double dt,
+                              int kind, double omega, double trt_magic, int nsteps);
 /* src/benchmarks/taylor_green.f90:51-84.  ref_loop=1 reproduces the reference
  * inner loop bound `y = 1, self%nx` (:68); ref_loop=0 loops y = 1, ny. */
 void oref_taylor_green_eval(int nx, int ny, double kx, double ky, double umax, double nu,

@@ -236,6 +236,21 @@ extern "C" int plbm_set_collision(plbm_grid_t* g, int kind) {
   return PLBM_OK;
 }
 
+extern "C" int plbm_set_time_step(plbm_grid_t* g, double dt) {
+  if (int r = check_grid(g)) return r;
+  if (!(dt > 0.0)) return fail(PLBM_E_INVALID, "dt = %g must be > 0", dt);
+  g->dt = dt;
+  return PLBM_OK;
+}
+
+extern "C" int plbm_set_streaming(plbm_grid_t* g, int scheme) {
+  if (int r = check_grid(g)) return r;
+  if (scheme < PLBM_STREAM_LBM || scheme > PLBM_STREAM_FDM_SOFONEA)
+    return fail(PLBM_E_INVALID, "unknown streaming scheme %d", scheme);
+  g->streaming = scheme;
+  return PLBM_OK;
+}
+
 extern "C" int plbm_set_math(plbm_grid_t* g, int math) {
   if (int r = check_grid(g)) return r;
   if (math < PLBM_MATH_FMA || math > PLBM_MATH_DF64) return fail(PLBM_E_INVALID, "unknown math mode %d", math);
@@ -309,9 +324,20 @@ extern "C" int plbm_set_pdf_to_equilibrium(plbm_grid_t* g, const double* rho, co
 
 namespace {
 
+// Finite-volume / finite-difference streaming of the handle's scheme.
+cudaError_t stream_scheme(const plbm_grid_t* g, const Sweep& s) {
+  return g->math == PLBM_MATH_STRICT ? strict::stream_scheme_f64(g->streaming, s, g->dt)
+                                     : fma::stream_scheme_f64(g->streaming, s, g->dt);
+}
+
 // One fused step from lattice a to lattice b with the handle's settings.
 cudaError_t fused_step(plbm_grid_t* g, const void* a, void* b, const CollParams& p) {
   Sweep s{g->nx, g->ny, g->ld, a, b, g->stream};
+  if (g->streaming != PLBM_STREAM_LBM) {  // the scheme's kernel, then the collision
+    cudaError_t e = stream_scheme(g, s);
+    if (e != cudaSuccess) return e;
+    return g->math == PLBM_MATH_STRICT ? strict::collide_f64(g->kind, s, p) : fma::collide_f64(g->kind, s, p);
+  }
   if (g->storage != PLBM_F64) {
     if (g->math == PLBM_MATH_FMA) return step_pull_dev(g->storage, g->kind, s, p);
     return step_pull_dev_hi(g->storage, g->math, g->kind, s, p);
@@ -330,12 +356,27 @@ cudaError_t fused_step(plbm_grid_t* g, const void* a, void* b, const CollParams&
   }
 }
 
+// The finite-volume / finite-difference schemes: binary64 storage, FMA or
+// strict arithmetic.
+int check_scheme(const plbm_grid_t* g) {
+  if (g->streaming == PLBM_STREAM_LBM) return PLBM_OK;
+  if (g->storage != PLBM_F64) return fail(PLBM_E_UNSUPPORTED, "streaming scheme %d needs PLBM_F64 storage", g->streaming);
+  if (g->math != PLBM_MATH_FMA && g->math != PLBM_MATH_STRICT)
+    return fail(PLBM_E_UNSUPPORTED, "streaming scheme %d runs with PLBM_MATH_FMA or PLBM_MATH_STRICT", g->streaming);
+  return PLBM_OK;
+}
+
 }  // namespace
 
 extern "C" int plbm_stream(plbm_grid_t* g) {
   if (int r = check_grid(g)) return r;
   if (int r = use_device(g)) return r;
   Sweep s{g->nx, g->ny, g->ld, lattice(g, g->iold), lattice(g, g->inew), g->stream};
+  if (g->streaming != PLBM_STREAM_LBM) {
+    if (int r = check_scheme(g)) return r;
+    CUDA_TRY(stream_scheme(g, s), "streaming-scheme kernel");
+    return ok();
+  }
   cudaError_t e = g->storage == PLBM_F64 ? fma::stream_f64(s) : stream_dev(g->storage, s);
   if (e != cudaSuccess) return cuda_fail(e, "lbm_stream kernel");
   return ok();
@@ -361,6 +402,7 @@ extern "C" int plbm_perform_lbm_step(plbm_grid_t* g, int nsteps) {
     return fail(PLBM_E_UNSUPPORTED, "PLBM_MATH_HYBRID is not offered for collide_bgk_improved");
   if (g->storage != PLBM_F64 && (g->math == PLBM_MATH_HYBRID || g->math == PLBM_MATH_DF64) && g->kind != PLBM_BGK)
     return fail(PLBM_E_UNSUPPORTED, "PLBM_MATH_HYBRID / PLBM_MATH_DF64 with deviation storage are offered for collide_bgk only");
+  if (int r = check_scheme(g)) return r;
   if (int r = use_device(g)) return r;
   const CollParams p = plbm_make_params(g->omega, g->trt_magic);
   for (int i = 0; i < nsteps; i++) {
@@ -399,9 +441,10 @@ extern "C" int plbm_perform_triple_step(plbm_grid_t* g, int nsteps) {
     void* pre = physical(g, g->spare_slot);
     Sweep s{g->nx, g->ny, g->ld, lattice(g, g->iold), lattice(g, g->inew), g->stream};
     cudaError_t e;
-    if (g->kind == PLBM_BGKI && g->ld != g->ny) {
-      // the (ny,nx,0:8) dummy of collide_bgk_improved: the reference's passes
-      e = fma::stream_f64(s);
+    if (g->streaming != PLBM_STREAM_LBM || (g->kind == PLBM_BGKI && g->ld != g->ny)) {
+      // another streaming scheme, or the (ny,nx,0:8) dummy of
+      // collide_bgk_improved: the reference's passes
+      e = g->streaming != PLBM_STREAM_LBM ? stream_scheme(g, s) : fma::stream_f64(s);
       if (e == cudaSuccess)
         e = cudaMemcpyAsync(pre, s.dst, g->lat_elems * g->elem_bytes, cudaMemcpyDeviceToDevice, g->stream);
       if (e == cudaSuccess) e = strict_math ? strict::collide_f64(g->kind, s, p) : fma::collide_f64(g->kind, s, p);

@@ -24,6 +24,7 @@ constexpr int kMaxLattices = 16;
 struct plbm_grid {
   int nx, ny, ld, nf, storage;
   int kind = PLBM_BGK, math = PLBM_MATH_FMA;
+  int streaming = PLBM_STREAM_LBM;    // grid%streaming
   int iold = 2, inew = 1, imid = -1;  // 1-based, as alloc_grid sets them
   double nu = 0, dt = 1, tau = 0, omega = 1, trt_magic = 0.25;
   int device = 0;

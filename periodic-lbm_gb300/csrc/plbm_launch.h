@@ -32,6 +32,9 @@ constexpr int kBlock = 256;
   cudaError_t step_push_shift_f64(int kind, const Sweep& s, const CollParams& p);         \
   /* perform_triple_step fused: also stores the pre-collision populations to pre */       \
   cudaError_t step_pull_pre_f64(int kind, const Sweep& s, void* pre, const CollParams& p); \
+  /* grid%streaming => stream_fvm_bardow (1), stream_fdm_bardow (2, 3 iso,    */          \
+  /* 4 least squares), stream_fdm_sofonea (5): src/fvm_bardow.F90:393-886     */          \
+  cudaError_t stream_scheme_f64(int scheme, const Sweep& s, double dt);                   \
   }
 PLBM_DECLARE_F64(fma)
 PLBM_DECLARE_F64(strict)

@@ -4,6 +4,8 @@
 !> hot path on the GPU through libplbmgpu.so (C ABI: include/plbm_gpu.h):
 !>
 !>   lbm_stream_gpu(grid)       streaming_interface, src/periodic_lbm.f90:32-43
+!>   stream_fvm_bardow_gpu(grid), stream_fdm_bardow_gpu(grid),
+!>   stream_fdm_sofonea_gpu(grid)  streaming_interface, src/fvm_bardow.F90:393,511,688
 !>   collide_bgk_gpu(grid)      collision_interface, src/collision_bgk.F90:17
 !>   collide_trt_gpu(grid)      collision_interface, src/collision_trt.F90:41
 !>   collide_rr_gpu(grid)       collision_interface, src/collision_regularized.F90:21
@@ -40,6 +42,7 @@ module plbm_gpu
    public :: plbm_gpu_attach, plbm_gpu_detach, plbm_gpu_upload, plbm_gpu_download
    public :: lbm_stream_gpu, perform_lbm_step_gpu, update_macros_gpu
    public :: perform_triple_step_gpu, output_npy_gpu
+   public :: stream_fvm_bardow_gpu, stream_fdm_bardow_gpu, stream_fdm_sofonea_gpu
    public :: collide_bgk_gpu, collide_trt_gpu, collide_rr_gpu, collide_bgk_improved_gpu
    public :: PLBM_MATH_FMA, PLBM_MATH_STRICT, PLBM_MATH_HYBRID
 
@@ -109,6 +112,16 @@ module plbm_gpu
       end function
       type(c_ptr) function plbm_last_error() bind(c, name="plbm_last_error")
          import :: c_ptr
+      end function
+      integer(c_int) function plbm_set_streaming(g, scheme) bind(c, name="plbm_set_streaming")
+         import :: c_int, c_ptr
+         type(c_ptr), value :: g
+         integer(c_int), value :: scheme
+      end function
+      integer(c_int) function plbm_set_time_step(g, dt) bind(c, name="plbm_set_time_step")
+         import :: c_int, c_ptr, c_double
+         type(c_ptr), value :: g
+         real(c_double), value :: dt
       end function
       integer(c_int) function plbm_grid_set_indices3(g, iold, inew, imid) bind(c, name="plbm_grid_set_indices3")
          import :: c_int, c_ptr
@@ -244,6 +257,36 @@ contains
       h = handle_of(grid)
       call sync_state(grid, h, -1_c_int)
       call check(plbm_stream(h), "plbm_stream")
+   end subroutine
+
+   subroutine stream_scheme(grid, scheme)
+      class(lattice_grid), intent(inout) :: grid
+      integer(c_int), intent(in) :: scheme
+      type(c_ptr) :: h
+      h = handle_of(grid)
+      call sync_state(grid, h, -1_c_int)
+      call check(plbm_set_time_step(h, real(grid%dt, c_double)), "plbm_set_time_step")
+      call check(plbm_set_streaming(h, scheme), "plbm_set_streaming")
+      call check(plbm_stream(h), "plbm_stream")
+      call check(plbm_set_streaming(h, 0_c_int), "plbm_set_streaming")
+   end subroutine
+
+   !> streaming_interface: stream_fvm_bardow on the device (grid%dt).
+   subroutine stream_fvm_bardow_gpu(grid)
+      class(lattice_grid), intent(inout) :: grid
+      call stream_scheme(grid, 1_c_int)
+   end subroutine
+
+   !> streaming_interface: stream_fdm_bardow (central differences) on the device.
+   subroutine stream_fdm_bardow_gpu(grid)
+      class(lattice_grid), intent(inout) :: grid
+      call stream_scheme(grid, 2_c_int)
+   end subroutine
+
+   !> streaming_interface: stream_fdm_sofonea on the device.
+   subroutine stream_fdm_sofonea_gpu(grid)
+      class(lattice_grid), intent(inout) :: grid
+      call stream_scheme(grid, 5_c_int)
    end subroutine
 
    subroutine collide_kind(grid, kind)

@@ -32,6 +32,10 @@ STORAGES = {"f64": F64, "f32dev": F32DEV, "f16dev": F16DEV}
 MATH_FMA, MATH_STRICT, MATH_HYBRID, MATH_DF64 = 0, 1, 2, 3
 MATHS = {"fma": MATH_FMA, "strict": MATH_STRICT, "hybrid": MATH_HYBRID, "df64": MATH_DF64}
 
+# streaming schemes (grid%streaming)
+SCHEMES = {"lbm": 0, "fvm_bardow": 1, "fdm_bardow": 2, "fdm_bardow_iso": 3, "fdm_bardow_wls": 4,
+           "fdm_sofonea": 5}
+
 F16_SCALE_LOG2 = 15
 
 _ERRNAMES = {
@@ -81,6 +85,8 @@ SIGNATURES = {
     "plbm_set_relaxation": (C.c_int, [_vp, C.c_double, C.c_double]),
     "plbm_set_collision": (C.c_int, [_vp, C.c_int]),
     "plbm_set_math": (C.c_int, [_vp, C.c_int]),
+    "plbm_set_streaming": (C.c_int, [_vp, C.c_int]),
+    "plbm_set_time_step": (C.c_int, [_vp, C.c_double]),
     "plbm_upload": (C.c_int, [_vp, _vp, C.c_int]),
     "plbm_download": (C.c_int, [_vp, _vp, C.c_int]),
     "plbm_set_pdf_to_equilibrium": (C.c_int, [_vp, _vp, _vp, _vp]),

@@ -9,6 +9,7 @@ reference                               here
 ``alloc_grid(grid,nx,ny,nf)``           ``LatticeGrid(nx, ny, nf)``
 ``set_properties(grid,nu,dt,magic)``    ``grid.set_properties(nu, dt, magic)``
 ``grid%collision => collide_rr``        ``grid.collision = "rr"``
+``grid%streaming => stream_fvm_bardow`` ``grid.streaming = "fvm_bardow"``
 ``set_pdf_to_equilibrium(grid)``        ``grid.set_pdf_to_equilibrium(rho, ux, uy)``
 ``perform_lbm_step(grid)``              ``grid.perform_lbm_step(nsteps=1)``
 ``grid%streaming()`` / ``collision()``  ``grid.stream()`` / ``grid.collide()``
@@ -48,7 +49,7 @@ class LatticeGrid:
     """A D2Q9 periodic lattice on the GPU with the reference's semantics."""
 
     def __init__(self, nx: int, ny: int, nf: int = 2, storage: str | int = "f64",
-                 collision: str | int = "bgk", math: str | int = "fma"):
+                 collision: str | int = "bgk", math: str | int = "fma", streaming: str | int = "lbm"):
         self._lib = _lib.load()
         st = _lib.STORAGES[storage] if isinstance(storage, str) else int(storage)
         h = C.c_void_p()
@@ -58,6 +59,7 @@ class LatticeGrid:
         self.ld = pad16(self.ny)
         self.collision = collision
         self.math = math
+        self.streaming = streaming
 
     # -- lifecycle ------------------------------------------------------------
     def close(self) -> None:
@@ -104,10 +106,27 @@ class LatticeGrid:
         check(self._lib.plbm_set_math(self.handle, v))
         self._math = v
 
+    @property
+    def streaming(self) -> int:
+        return self._streaming
+
+    @streaming.setter
+    def streaming(self, scheme) -> None:
+        """grid%streaming => lbm_stream | stream_fvm_bardow | stream_fdm_bardow[_iso|_wls] |
+        stream_fdm_sofonea ("lbm", "fvm_bardow", "fdm_bardow", "fdm_bardow_iso",
+        "fdm_bardow_wls", "fdm_sofonea")."""
+        v = _lib.SCHEMES[scheme] if isinstance(scheme, str) else int(scheme)
+        check(self._lib.plbm_set_streaming(self.handle, v))
+        self._streaming = v
+
     def set_properties(self, nu: float, dt: float, magic: float | None = None) -> None:
         """set_properties, src/fvm_bardow.F90:242-269."""
         mp = C.byref(C.c_double(magic)) if magic is not None else None
         check(self._lib.plbm_set_properties(self.handle, float(nu), float(dt), mp))
+
+    def set_time_step(self, dt: float) -> None:
+        """grid%dt alone (the finite-volume / finite-difference schemes' time step)."""
+        check(self._lib.plbm_set_time_step(self.handle, float(dt)))
 
     def set_relaxation(self, omega: float, trt_magic: float = 0.25) -> None:
         check(self._lib.plbm_set_relaxation(self.handle, float(omega), float(trt_magic)))

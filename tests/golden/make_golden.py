@@ -260,6 +260,79 @@ def sim_macros(h):
     return rho, u, v
 
 
+# --- src/fvm_bardow.F90:393-886: finite-volume / finite-difference streaming,
+# per population q on the (nx, ny) block; neighbours by rolls (whole grid).
+def _nbrs(a):
+    sh = lambda dx, dy: np.roll(a, shift=(-dx, -dy), axis=(0, 1))  # a[x+dx, y+dy]  # noqa: E731
+    return dict(c=a, e=sh(1, 0), n=sh(0, 1), w=sh(-1, 0), s=sh(0, -1), ne=sh(1, 1), nw=sh(-1, 1),
+                sw=sh(-1, -1), se=sh(1, -1))
+
+
+def stream_fvm(f, ny, dt):
+    g = f.copy()
+    p2, p8 = 0.5, 0.125
+    for q in range(1, 9):
+        cxq, cyq = dt * CX[q], dt * CY[q]
+        n = _nbrs(f[q, :, :ny])
+        fc, fe, fn, fw, fs = n["c"], n["e"], n["n"], n["w"], n["s"]
+        fne, fnw, fsw, fse = n["ne"], n["nw"], n["sw"], n["se"]
+        cfw = p2 * (fc + fw) - p2 * cxq * (fc - fw) - p8 * cyq * (fnw + fn - fsw - fs)
+        cfn = p2 * (fc + fn) - p2 * cyq * (fn - fc) - p8 * cxq * (fne + fe - fnw - fw)
+        cfe = p2 * (fc + fe) - p2 * cxq * (fe - fc) - p8 * cyq * (fne + fn - fse - fs)
+        cfs = p2 * (fc + fs) - p2 * cyq * (fc - fs) - p8 * cxq * (fse + fe - fsw - fw)
+        g[q, :, :ny] = fc - cxq * (cfe - cfw) - cyq * (cfn - cfs)
+    return g
+
+
+def stream_fdm(f, ny, dt, variant):
+    g = f.copy()
+    p2 = 0.5
+    t3, s6, f6, t12, o3 = 2.0 / 3.0, 1.0 / 6.0, 10.0 / 12.0, 1.0 / 12.0, 1.0 / 3.0
+    for q in range(1, 9):
+        cxq, cyq = dt * CX[q], dt * CY[q]
+        cxxq, cyyq, cxyq = 0.5 * cxq * cxq, 0.5 * cyq * cyq, cxq * cyq
+        n = _nbrs(f[q, :, :ny])
+        fc, fe, fn, fw, fs = n["c"], n["e"], n["n"], n["w"], n["s"]
+        fne, fnw, fsw, fse = n["ne"], n["nw"], n["sw"], n["se"]
+        if variant == "iso":
+            dfx = p2 * (s6 * (fne - fnw) + t3 * (fe - fw) + s6 * (fse - fsw))
+            dfy = p2 * (s6 * (fne - fse) + t3 * (fn - fs) + s6 * (fnw - fsw))
+            dfxx = t12 * (fne - 2 * fn + fnw) + f6 * (fe - 2 * fc + fw) + t12 * (fse - 2 * fs + fsw)
+            dfyy = t12 * (fne - 2 * fe + fse) + f6 * (fn - 2 * fc + fs) + t12 * (fnw - 2 * fw + fsw)
+            dfxy = 0.25 * (fne - fse - fnw + fsw)
+        elif variant == "wls":
+            dfx = s6 * ((fne - fnw) + (fe - fw) + (fse - fsw))
+            dfy = s6 * ((fne - fse) + (fn - fs) + (fnw - fsw))
+            dfxx = o3 * (fne - 2 * fn + fnw) + o3 * (fe - 2 * fc + fw) + o3 * (fse - 2 * fs + fsw)
+            dfyy = o3 * (fne - 2 * fe + fse) + o3 * (fn - 2 * fc + fs) + o3 * (fnw - 2 * fw + fsw)
+            dfxy = 0.25 * (fne - fnw + fsw - fse)
+        else:
+            dfx = p2 * (fe - fw)
+            dfy = p2 * (fn - fs)
+            dfxx = fe - 2 * fc + fw
+            dfyy = fn - 2 * fc + fs
+            dfxy = 0.25 * (fne - fse - fnw + fsw)
+        g[q, :, :ny] = fc - cxq * dfx - cyq * dfy + (cxxq * dfxx + cxyq * dfxy + cyyq * dfyy)
+    return g
+
+
+def stream_sofonea(f, ny, dt):
+    g = f.copy()
+    p2 = 0.5 / math.sqrt(2.0)
+    for q in range(1, 9):
+        a = f[q, :, :ny]
+        fu = np.roll(a, shift=(-CX[q], -CY[q]), axis=(0, 1))  # f(x + c)
+        fd = np.roll(a, shift=(CX[q], CY[q]), axis=(0, 1))    # f(x - c)
+        if q <= 4:
+            du1 = 0.5 * (fu - fd)
+            du2 = fu - 2 * a + fd
+        else:
+            du1 = p2 * (fu - fd)
+            du2 = 0.5 * (fu - 2 * a + fd)
+        g[q, :, :ny] = a + dt * (0.5 * dt * du2 - du1)
+    return g
+
+
 def perturbed_equilibrium(nx, ny, rng, amp=1e-3, noise=1e-5):
     ld = pad16(ny)
     k = 2 * math.pi
@@ -325,6 +398,23 @@ def main():
     nu = 0.1 / 3.0
     tau = 3.0 * nu
     g["props"] = np.array([tau, 1.0 / (tau + 0.5 * 1.0), (tau / 1.0) ** 2, lambda_d(1.25, 0.25)])
+    # streaming schemes, one application and 5 steps with BGK (own seed: the
+    # entries above do not change when these are added)
+    srng = np.random.default_rng(20240502)
+    for nx, ny in [(17, 13), (16, 16)]:
+        tag = f"{nx}x{ny}"
+        _, _, _, f0 = perturbed_equilibrium(nx, ny, srng)
+        g[f"schemes_{tag}_f0"] = f0
+        for name, fn in [("fvm_bardow", lambda f: stream_fvm(f, ny, 0.7)),
+                         ("fdm_bardow", lambda f: stream_fdm(f, ny, 0.7, "")),
+                         ("fdm_bardow_iso", lambda f: stream_fdm(f, ny, 0.7, "iso")),
+                         ("fdm_bardow_wls", lambda f: stream_fdm(f, ny, 0.7, "wls")),
+                         ("fdm_sofonea", lambda f: stream_sofonea(f, ny, 0.7))]:
+            g[f"schemes_{tag}_{name}"] = fn(f0)
+            f = f0.copy()
+            for _ in range(5):
+                f = bgk(fn(f), ny, 1.1)
+            g[f"schemes_{tag}_{name}_bgk5"] = f
     np.savez_compressed(OUT, **g)
     print(f"wrote {OUT} ({OUT.stat().st_size} bytes, {len(g)} arrays)")
 
