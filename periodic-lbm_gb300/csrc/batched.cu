@@ -188,6 +188,18 @@ __global__ void __launch_bounds__(kBatchMaxThreads) k_batch_step(const BatchGrid
   sweep<S, false, I>(grids, tile_start, tile_grid, ntiles, parity, base);
 }
 
+// The same for 128-thread CTAs with at least 6 resident per SM (at most 80
+// registers).  The binary64 hybrid tiles otherwise take 97 registers and 20
+// resident warps per SM; with the cap (a few bytes of spills) the 512-grid
+// batch runs 22 % faster.
+template <class S, typename I>
+__global__ void __launch_bounds__(128, 6) k_batch_step_128(const BatchGrid* __restrict__ grids,
+                                                          const int* __restrict__ tile_start,
+                                                          const int* __restrict__ tile_grid, int ntiles, int parity,
+                                                          typename S::elem* base) {
+  sweep<S, false, I>(grids, tile_start, tile_grid, ntiles, parity, base);
+}
+
 template <class S, typename I>
 cudaError_t launch_batch(const BatchLaunch& L, int nsteps, int parity0) {
   typedef typename S::elem E;
@@ -207,9 +219,14 @@ cudaError_t launch_batch(const BatchLaunch& L, int nsteps, int parity0) {
                               parity0, base, ctrl);
   }
   // one tile per CTA
+  const bool capped = L.threads == 128;
   for (int s = 0; s < nsteps; s++) {
-    k_batch_step<S, I><<<L.ntiles, L.threads, 0, L.stream>>>(L.grids, L.tile_start, L.tile_grid, L.ntiles,
-                                                             (parity0 + s) & 1, base);
+    if (capped)
+      k_batch_step_128<S, I><<<L.ntiles, L.threads, 0, L.stream>>>(L.grids, L.tile_start, L.tile_grid, L.ntiles,
+                                                                   (parity0 + s) & 1, base);
+    else
+      k_batch_step<S, I><<<L.ntiles, L.threads, 0, L.stream>>>(L.grids, L.tile_start, L.tile_grid, L.ntiles,
+                                                               (parity0 + s) & 1, base);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
