@@ -110,11 +110,17 @@ __device__ __noinline__ void hybrid_fallback_cell(const double* __restrict__ src
   g_hybrid_range_flag = 1;
 }
 
+// Resident CTAs per SM the hybrid kernels are compiled for (register cap
+// 65536 / (256 x this)): measured best at 8192^2 -- TRT 4 (64 registers, +6 %
+// over the uncapped kernel), BGK and RR 5 (48 registers, +2 to +4 %, a few
+// bytes of spills).
+constexpr int hybrid_min_blocks(int kind) { return kind == K_TRT ? 4 : 5; }
+
 // I: index type of the lattice offsets; 32-bit when the whole lattice has
 // fewer than 2^32 elements (one multiply-add per address instead of 64-bit
 // arithmetic).
 template <typename I, int KIND>
-__global__ void __launch_bounds__(kBlock) k_step_hybrid(const double* __restrict__ src, double* __restrict__ dst,
+__global__ void __launch_bounds__(kBlock, hybrid_min_blocks(KIND)) k_step_hybrid(const double* __restrict__ src, double* __restrict__ dst,
                                                        int nx, int ny, int ld, int ftiles, HybridArgs a) {
   const int x = blockIdx.x / ftiles;
   const int y = (blockIdx.x - x * ftiles) * blockDim.x + threadIdx.x;
