@@ -333,7 +333,12 @@ cudaError_t stream_scheme(const plbm_grid_t* g, const Sweep& s) {
 // One fused step from lattice a to lattice b with the handle's settings.
 cudaError_t fused_step(plbm_grid_t* g, const void* a, void* b, const CollParams& p) {
   Sweep s{g->nx, g->ny, g->ld, a, b, g->stream};
-  if (g->streaming != PLBM_STREAM_LBM) {  // the scheme's kernel, then the collision
+  if (g->streaming != PLBM_STREAM_LBM) {
+    // FMA arithmetic: one fused kernel, the scheme in stencil form then the
+    // collision; strict: the reference's two passes, expression by expression
+    if (g->math == PLBM_MATH_FMA && !(g->kind == PLBM_BGKI && g->ld != g->ny))
+      return fma::step_scheme_f64(g->streaming, g->kind, s, g->dt, p);
+    if (g->math == PLBM_MATH_HYBRID) return step_scheme_hybrid(g->streaming, g->kind, s, g->dt, p);
     cudaError_t e = stream_scheme(g, s);
     if (e != cudaSuccess) return e;
     return g->math == PLBM_MATH_STRICT ? strict::collide_f64(g->kind, s, p) : fma::collide_f64(g->kind, s, p);
@@ -361,8 +366,10 @@ cudaError_t fused_step(plbm_grid_t* g, const void* a, void* b, const CollParams&
 int check_scheme(const plbm_grid_t* g) {
   if (g->streaming == PLBM_STREAM_LBM) return PLBM_OK;
   if (g->storage != PLBM_F64) return fail(PLBM_E_UNSUPPORTED, "streaming scheme %d needs PLBM_F64 storage", g->streaming);
-  if (g->math != PLBM_MATH_FMA && g->math != PLBM_MATH_STRICT)
-    return fail(PLBM_E_UNSUPPORTED, "streaming scheme %d runs with PLBM_MATH_FMA or PLBM_MATH_STRICT", g->streaming);
+  if (g->math == PLBM_MATH_HYBRID && g->kind == PLBM_BGKI)
+    return fail(PLBM_E_UNSUPPORTED, "PLBM_MATH_HYBRID is not offered for collide_bgk_improved");
+  if (g->math != PLBM_MATH_FMA && g->math != PLBM_MATH_STRICT && g->math != PLBM_MATH_HYBRID)
+    return fail(PLBM_E_UNSUPPORTED, "streaming scheme %d runs with PLBM_MATH_FMA, _STRICT or _HYBRID", g->streaming);
   return PLBM_OK;
 }
 

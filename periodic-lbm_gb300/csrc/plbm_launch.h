@@ -35,6 +35,8 @@ constexpr int kBlock = 256;
   /* grid%streaming => stream_fvm_bardow (1), stream_fdm_bardow (2, 3 iso,    */          \
   /* 4 least squares), stream_fdm_sofonea (5): src/fvm_bardow.F90:393-886     */          \
   cudaError_t stream_scheme_f64(int scheme, const Sweep& s, double dt);                   \
+  /* the same fused with collide_* in stencil form (9 FMAs per population) */             \
+  cudaError_t step_scheme_f64(int scheme, int kind, const Sweep& s, double dt, const CollParams& p); \
   }
 PLBM_DECLARE_F64(fma)
 PLBM_DECLARE_F64(strict)
@@ -42,6 +44,9 @@ PLBM_DECLARE_F64(strict)
 
 // binary64 storage, hybrid arithmetic (hybrid.cuh), YFast pull, BGK, TRT and RR
 cudaError_t step_pull_df64(int kind, const Sweep& s, const CollParams& p);
+// A finite-volume / finite-difference streaming scheme (stencil form) fused
+// with the hybrid collision (BGK, TRT, RR).
+cudaError_t step_scheme_hybrid(int scheme, int kind, const Sweep& s, double dt, const CollParams& p);
 cudaError_t hybrid_range_flag(int* flag, int reset);
 
 // Deviation storage (storage = 1 float, 2 half), binary32 arithmetic.

@@ -13,6 +13,7 @@
 #include "coll_df64.cuh"
 #include "hybrid.cuh"
 #include "plbm_launch.h"
+#include "schemes.cuh"
 
 namespace plbm {
 
@@ -152,6 +153,42 @@ __global__ void __launch_bounds__(kBlock, hybrid_min_blocks(KIND)) k_step_hybrid
   for (int q = 0; q < 9; q++) dst[(I)q * P + o] = f[q];
 }
 
+// A finite-volume / finite-difference streaming scheme in stencil form fused
+// with the hybrid collision (binary64 storage).  Out-of-range cells take the
+// binary64 collision (out of line, the stencil evaluated again).
+template <int TAPS, int KIND>
+__device__ __noinline__ void scheme_fallback_cell(const double* __restrict__ src, double* __restrict__ dst, int x,
+                                                  int y, int nx, int ny, int ld, const sch::Stencil& st,
+                                                  const CollParams& p) {
+  double f[9];
+  sch::stencil_pull<YFast, TAPS>(src, x, y, nx, ny, ld, st, f);
+  collide_ref<KIND>(f, p);
+#pragma unroll
+  for (int q = 0; q < 9; q++) dst[YFast::off(x, y, q, nx, ny, ld)] = f[q];
+  g_hybrid_range_flag = 1;
+}
+
+template <int TAPS, int KIND>
+__global__ void __launch_bounds__(kBlock) k_step_scheme_hybrid(const double* __restrict__ src,
+                                                              double* __restrict__ dst, int nx, int ny, int ld,
+                                                              int ftiles, sch::Stencil st, HybridArgs a) {
+  const int x = blockIdx.x / ftiles;
+  const int y = (blockIdx.x - x * ftiles) * blockDim.x + threadIdx.x;
+  if (y >= ny) return;
+  double f[9];
+  sch::stencil_pull<YFast, TAPS>(src, x, y, nx, ny, ld, st, f);
+  bool bad = false;
+  if (KIND == K_TRT) hy::trt_fast(f, a.trt, bad);
+  else if (KIND == K_RR) hy::rr_fast(f, a.rr, bad);
+  else hy::bgk_fast(f, a.bgk, bad);
+  if (bad) {
+    scheme_fallback_cell<TAPS, KIND>(src, dst, x, y, nx, ny, ld, st, a.ref);
+    return;
+  }
+#pragma unroll
+  for (int q = 0; q < 9; q++) dst[YFast::off(x, y, q, nx, ny, ld)] = f[q];
+}
+
 template <int KIND>
 cudaError_t launch_hybrid(const Sweep& s, unsigned blocks, int ft, const HybridArgs& a) {
   const double* src = static_cast<const double*>(s.src);
@@ -220,6 +257,36 @@ cudaError_t step_pull_df64(int kind, const Sweep& s, const CollParams& cp) {
   if (kind == K_TRT) return launch_hybrid<K_TRT>(s, (unsigned)blocks, ft, a);
   if (kind == K_RR) return launch_hybrid<K_RR>(s, (unsigned)blocks, ft, a);
   return launch_hybrid<K_BGK>(s, (unsigned)blocks, ft, a);
+}
+
+cudaError_t step_scheme_hybrid(int scheme, int kind, const Sweep& s, double dt, const CollParams& cp) {
+  if (kind != K_BGK && kind != K_TRT && kind != K_RR) return cudaErrorNotSupported;
+  if (scheme < sch::FVM || scheme > sch::SOFONEA) return cudaErrorInvalidValue;
+  const int ft = (s.ny + kBlock - 1) / kBlock;
+  const long long blocks = (long long)ft * s.nx;
+  if (blocks <= 0 || blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+  const sch::Stencil st = sch::stencil_coefficients(scheme, dt);
+  HybridArgs a;
+  a.bgk = hybrid_params(cp.omega);
+  a.trt = hybrid_trt_params(cp);
+  a.rr = hybrid_rr_params(cp);
+  a.ref = cp;
+  const double* src = static_cast<const double*>(s.src);
+  double* dst = static_cast<double*>(s.dst);
+  const unsigned nb = (unsigned)blocks;
+#define PLBM_SCH_HY(T)                                                                                        \
+  switch (kind) {                                                                                             \
+    case K_BGK: k_step_scheme_hybrid<T, K_BGK><<<nb, kBlock, 0, s.stream>>>(src, dst, s.nx, s.ny, s.ld, ft, st, a); break; \
+    case K_TRT: k_step_scheme_hybrid<T, K_TRT><<<nb, kBlock, 0, s.stream>>>(src, dst, s.nx, s.ny, s.ld, ft, st, a); break; \
+    default: k_step_scheme_hybrid<T, K_RR><<<nb, kBlock, 0, s.stream>>>(src, dst, s.nx, s.ny, s.ld, ft, st, a); break;     \
+  }
+  switch (sch::taps_of(scheme)) {
+    case sch::TAPS_LINE: PLBM_SCH_HY(sch::TAPS_LINE) break;
+    case sch::TAPS_AXIS3: PLBM_SCH_HY(sch::TAPS_AXIS3) break;
+    default: PLBM_SCH_HY(sch::TAPS_FULL) break;
+  }
+#undef PLBM_SCH_HY
+  return cudaGetLastError();
 }
 
 cudaError_t step_pull_dev_hi(int storage, int math, int kind, const Sweep& s, const CollParams& cp) {

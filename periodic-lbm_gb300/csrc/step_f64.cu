@@ -19,6 +19,7 @@
 //   k_step<XFast, push>   the plugin step of sim/sim.F90:404-505 + :568-624:
 //                         shifted populations, collide, then push along c_i.
 #include "plbm_launch.h"
+#include "schemes.cuh"
 
 #ifdef PLBM_STRICT
 #define PLBM_NS strict
@@ -93,83 +94,39 @@ __global__ void __launch_bounds__(kBlock) k_step_pre(const double* __restrict__ 
 }
 
 // Finite-volume / finite-difference streaming (src/fvm_bardow.F90:393-886),
-// one thread per cell, populations 1..8; each population's new value is a
-// 9-point (FVM, FDM) or 3-point (Sofonea) stencil of the same population.
-// The arithmetic is the Fortran's expression by expression (the strict build
-// reproduces it exactly).  Loops cover the whole nx x ny grid.
-enum { SCH_FVM = 1, SCH_FDM = 2, SCH_FDM_ISO = 3, SCH_FDM_WLS = 4, SCH_SOFONEA = 5 };
-
-template <int SCHEME>
-__device__ __forceinline__ double scheme_cell(const double* __restrict__ a, int q, int x, int y, int xp, int xm,
-                                              int yp, int ym, int nx, int ny, int ld, double dt) {
-  auto at = [&](int yy, int xx) { return __ldg(a + YFast::off(xx, yy, q, nx, ny, ld)); };
-  const double cxq = dt * (double)cx_of(q), cyq = dt * (double)cy_of(q);
-  if (SCHEME == SCH_SOFONEA) {
-    const int cxi = cx_of(q), cyi = cy_of(q);
-    const int xu = cxi > 0 ? xp : (cxi < 0 ? xm : x), xd = cxi > 0 ? xm : (cxi < 0 ? xp : x);
-    const int yu = cyi > 0 ? yp : (cyi < 0 ? ym : y), yd = cyi > 0 ? ym : (cyi < 0 ? yp : y);
-    const double fc = at(y, x), fu = at(yu, xu), fd = at(yd, xd);
-    double du1, du2;
-    if (q <= 4) {
-      du1 = 0.5 * (fu - fd);
-      du2 = fu - 2 * fc + fd;
-    } else {
-      const double p2 = 0.35355339059327373;  // 0.5/sqrt(2) rounded to binary64
-      du1 = p2 * (fu - fd);
-      du2 = 0.5 * (fu - 2 * fc + fd);
-    }
-    return fc + dt * (0.5 * dt * du2 - du1);
-  }
-  const double fc = at(y, x), fe = at(y, xp), fn = at(yp, x), fw = at(y, xm), fs = at(ym, x);
-  const double fne = at(yp, xp), fnw = at(yp, xm), fsw = at(ym, xm), fse = at(ym, xp);
-  if (SCHEME == SCH_FVM) {
-    const double p2 = 0.5, p8 = 0.125;
-    const double cfw = p2 * (fc + fw) - p2 * cxq * (fc - fw) - p8 * cyq * (fnw + fn - fsw - fs);
-    const double cfn = p2 * (fc + fn) - p2 * cyq * (fn - fc) - p8 * cxq * (fne + fe - fnw - fw);
-    const double cfe = p2 * (fc + fe) - p2 * cxq * (fe - fc) - p8 * cyq * (fne + fn - fse - fs);
-    const double cfs = p2 * (fc + fs) - p2 * cyq * (fc - fs) - p8 * cxq * (fse + fe - fsw - fw);
-    return fc - cxq * (cfe - cfw) - cyq * (cfn - cfs);
-  }
-  const double cxxq = 0.5 * cxq * cxq, cyyq = 0.5 * cyq * cyq, cxyq = cxq * cyq;
-  double dfx, dfy, dfxx, dfyy, dfxy;
-  if (SCHEME == SCH_FDM_ISO) {
-    const double p2 = 0.5, two_thirds = 2.0 / 3.0, one_sixth = 1.0 / 6.0, five_sixths = 10.0 / 12.0,
-                 one_twelth = 1.0 / 12.0;
-    dfx = p2 * (one_sixth * (fne - fnw) + two_thirds * (fe - fw) + one_sixth * (fse - fsw));
-    dfy = p2 * (one_sixth * (fne - fse) + two_thirds * (fn - fs) + one_sixth * (fnw - fsw));
-    dfxx = one_twelth * (fne - 2 * fn + fnw) + five_sixths * (fe - 2 * fc + fw) + one_twelth * (fse - 2 * fs + fsw);
-    dfyy = one_twelth * (fne - 2 * fe + fse) + five_sixths * (fn - 2 * fc + fs) + one_twelth * (fnw - 2 * fw + fsw);
-    dfxy = 0.25 * (fne - fse - fnw + fsw);
-  } else if (SCHEME == SCH_FDM_WLS) {
-    const double one_sixth = 1.0 / 6.0, one_third = 1.0 / 3.0;
-    dfx = one_sixth * ((fne - fnw) + (fe - fw) + (fse - fsw));
-    dfy = one_sixth * ((fne - fse) + (fn - fs) + (fnw - fsw));
-    dfxx = one_third * (fne - 2 * fn + fnw) + one_third * (fe - 2 * fc + fw) + one_third * (fse - 2 * fs + fsw);
-    dfyy = one_third * (fne - 2 * fe + fse) + one_third * (fn - 2 * fc + fs) + one_third * (fnw - 2 * fw + fsw);
-    dfxy = 0.25 * (fne - fnw + fsw - fse);
-  } else {
-    dfx = 0.5 * (fe - fw);
-    dfy = 0.5 * (fn - fs);
-    dfxx = fe - 2 * fc + fw;
-    dfyy = fn - 2 * fc + fs;
-    dfxy = 0.25 * (fne - fse - fnw + fsw);
-  }
-  return fc - cxq * dfx - cyq * dfy + (cxxq * dfxx + cxyq * dfxy + cyyq * dfyy);
-}
-
-// grid%streaming => stream_fvm_bardow / stream_fdm_bardow / stream_fdm_sofonea.
-// The rest population of the finite-difference schemes (all ld rows) is
-// copied by the launcher; the finite-volume one copies rows 1:ny here.
+// one thread per cell, populations 1..8, each the reference's expression of
+// its 3x3 neighbourhood (sch::scheme_value; the strict build reproduces the
+// Fortran exactly).  The rest population of the finite-difference schemes
+// (all ld rows) is copied by the launcher; the finite-volume one copies rows
+// 1:ny here.
 template <int SCHEME>
 __global__ void __launch_bounds__(kBlock) k_stream_scheme(const double* __restrict__ src, double* __restrict__ dst,
                                                          int nx, int ny, int ld, int ftiles, double dt) {
   int x, y;
   if (!cell_of<YFast>(ftiles, nx, ny, x, y)) return;
   const int xp = wrap_p(x, nx), xm = wrap_m(x, nx), yp = wrap_p(y, ny), ym = wrap_m(y, ny);
-  if (SCHEME == SCH_FVM) dst[YFast::off(x, y, 0, nx, ny, ld)] = __ldg(src + YFast::off(x, y, 0, nx, ny, ld));
+  if (SCHEME == sch::FVM) dst[YFast::off(x, y, 0, nx, ny, ld)] = __ldg(src + YFast::off(x, y, 0, nx, ny, ld));
 #pragma unroll
-  for (int q = 1; q < 9; q++)
-    dst[YFast::off(x, y, q, nx, ny, ld)] = scheme_cell<SCHEME>(src, q, x, y, xp, xm, yp, ym, nx, ny, ld, dt);
+  for (int q = 1; q < 9; q++) {
+    double v[9];
+    sch::gather<YFast>(src, q, x, y, xp, xm, yp, ym, nx, ny, ld, v);
+    dst[YFast::off(x, y, q, nx, ny, ld)] = sch::scheme_value(SCHEME, v, q, dt);
+  }
+}
+
+// Fused stencil-form streaming + collide_* (FMA build): one read pass of the
+// 3x3 neighbourhoods (L1/L2 reuse), one write of the 9 collided populations.
+template <int TAPS, int KIND>
+__global__ void __launch_bounds__(kBlock) k_step_scheme(const double* __restrict__ src, double* __restrict__ dst,
+                                                       int nx, int ny, int ld, int ftiles, sch::Stencil st,
+                                                       CollParams p) {
+  int x, y;
+  if (!cell_of<YFast>(ftiles, nx, ny, x, y)) return;
+  double f[9];
+  sch::stencil_pull<YFast, TAPS>(src, x, y, nx, ny, ld, st, f);
+  collide_ref<KIND>(f, p);
+#pragma unroll
+  for (int q = 0; q < 9; q++) dst[YFast::off(x, y, q, nx, ny, ld)] = f[q];
 }
 
 // lbm_stream: fdst(y,x,q) = fsrc(y - cy, x - cx, q) for rows 1:ny.
@@ -270,18 +227,45 @@ cudaError_t stream_scheme_f64(int scheme, const Sweep& s, double dt) {
   const double* a = static_cast<const double*>(s.src);
   double* b = static_cast<double*>(s.dst);
   const unsigned nb = (unsigned)blocks;
-  if (scheme != SCH_FVM) {  // fnew(:,:,0) = fold(:,:,0), padding rows included
+  if (scheme != sch::FVM) {  // fnew(:,:,0) = fold(:,:,0), padding rows included
     cudaError_t e = cudaMemcpyAsync(b, a, sizeof(double) * (size_t)s.ld * s.nx, cudaMemcpyDeviceToDevice, s.stream);
     if (e != cudaSuccess) return e;
   }
   switch (scheme) {
-    case SCH_FVM: k_stream_scheme<SCH_FVM><<<nb, kBlock, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft, dt); break;
-    case SCH_FDM: k_stream_scheme<SCH_FDM><<<nb, kBlock, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft, dt); break;
-    case SCH_FDM_ISO: k_stream_scheme<SCH_FDM_ISO><<<nb, kBlock, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft, dt); break;
-    case SCH_FDM_WLS: k_stream_scheme<SCH_FDM_WLS><<<nb, kBlock, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft, dt); break;
-    case SCH_SOFONEA: k_stream_scheme<SCH_SOFONEA><<<nb, kBlock, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft, dt); break;
+    case sch::FVM: k_stream_scheme<sch::FVM><<<nb, kBlock, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft, dt); break;
+    case sch::FDM: k_stream_scheme<sch::FDM><<<nb, kBlock, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft, dt); break;
+    case sch::FDM_ISO: k_stream_scheme<sch::FDM_ISO><<<nb, kBlock, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft, dt); break;
+    case sch::FDM_WLS: k_stream_scheme<sch::FDM_WLS><<<nb, kBlock, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft, dt); break;
+    case sch::SOFONEA: k_stream_scheme<sch::SOFONEA><<<nb, kBlock, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft, dt); break;
     default: return cudaErrorInvalidValue;
   }
+  return cudaGetLastError();
+}
+
+cudaError_t step_scheme_f64(int scheme, int kind, const Sweep& s, double dt, const CollParams& p) {
+  const int ft = tiles(s.ny);
+  const long long blocks = (long long)ft * s.nx;
+  if (blocks <= 0 || blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+  if (kind == K_BGKI && s.ld != s.ny) return cudaErrorNotSupported;
+  const sch::Stencil st = sch::stencil_coefficients(scheme, dt);
+  const double* a = static_cast<const double*>(s.src);
+  double* b = static_cast<double*>(s.dst);
+  const unsigned nb = (unsigned)blocks;
+#define PLBM_SCH_KIND(SC)                                                                                     \
+  switch (kind) {                                                                                             \
+    case K_BGK: k_step_scheme<SC, K_BGK><<<nb, kBlock, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft, st, p); break; \
+    case K_TRT: k_step_scheme<SC, K_TRT><<<nb, kBlock, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft, st, p); break; \
+    case K_RR: k_step_scheme<SC, K_RR><<<nb, kBlock, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft, st, p); break;   \
+    case K_BGKI: k_step_scheme<SC, K_BGKI><<<nb, kBlock, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft, st, p); break; \
+    default: return cudaErrorInvalidValue;                                                                    \
+  }
+  if (scheme < sch::FVM || scheme > sch::SOFONEA) return cudaErrorInvalidValue;
+  switch (sch::taps_of(scheme)) {
+    case sch::TAPS_LINE: PLBM_SCH_KIND(sch::TAPS_LINE) break;
+    case sch::TAPS_AXIS3: PLBM_SCH_KIND(sch::TAPS_AXIS3) break;
+    default: PLBM_SCH_KIND(sch::TAPS_FULL) break;
+  }
+#undef PLBM_SCH_KIND
   return cudaGetLastError();
 }
 

@@ -85,6 +85,25 @@ def test_scheme_steps_fma_within_1e12(gpu_lib, scheme):
     g.close()
 
 
+@pytest.mark.parametrize("scheme", SCHEMES)
+@pytest.mark.parametrize("kind", ["bgk", "trt", "rr"])
+def test_scheme_steps_hybrid_within_1e12(gpu_lib, scheme, kind):
+    """The fused stencil-form scheme + hybrid collision against the oracle's
+    reference-expression scheme + collision."""
+    nx, ny = 48, 40
+    steps = 30 if scheme == "fdm_bardow_wls" else 80
+    f0 = state(nx, ny)
+    g = gpu_grid(nx, ny, scheme, kind, "hybrid", 0.3, 0.05, f0)
+    om, magic = g.omega, g.properties()["trt_magic"]
+    g.perform_lbm_step(steps)
+    got = g.download(g.iold)
+    f2 = np.stack([np.zeros_like(f0), f0.copy()])
+    iold, _ = O.perform_step_scheme(f2, ny, 2, 1, scheme, 0.3, KIND[kind], om, magic, steps)
+    for a, b in zip(O.update_macros(got, ny), O.update_macros(f2[iold - 1], ny)):
+        assert relinf(a, b) <= 1e-12
+    g.close()
+
+
 def test_scheme_triple_step_matches_oracle(gpu_lib):
     """perform_triple_step with grid%streaming => stream_fdm_bardow."""
     from plbm import LatticeGrid
@@ -120,7 +139,7 @@ def test_scheme_errors(gpu_lib):
         g.perform_lbm_step(1)
     assert e.value.code == -4
     g.close()
-    g = LatticeGrid(8, 8, math="hybrid", streaming="fvm_bardow")
+    g = LatticeGrid(8, 8, math="hybrid", collision="bgki", streaming="fvm_bardow")
     with pytest.raises(PlbmError) as e:
         g.perform_lbm_step(1)
     assert e.value.code == -4
