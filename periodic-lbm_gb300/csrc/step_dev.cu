@@ -43,6 +43,49 @@ __global__ void __launch_bounds__(kBlock) k_step_dev(const typename S::elem* __r
   }
 }
 
+// Relaxation constants of the shifted operators, rounded to binary32 once
+// on the host: BGK (omega), TRT (le, les, lds), RR (w (1 - omega) x 3).
+struct ShiftParamsF {
+  float a, b, c;
+};
+
+ShiftParamsF shift_params(int kind, const CollParams& p) {
+  if (kind == K_TRT) return {(float)p.omega, (float)p.les, (float)p.lds};
+  if (kind == K_RR) return {(float)p.rr_w0, (float)p.rr_ws, (float)p.rr_wd};
+  return {(float)p.omega, 0.0f, 0.0f};
+}
+
+// The pull step of the src/ layout (YFast) with explicit pull offsets: I is
+// the offset type, 32-bit when the lattice has fewer than 2^32 elements (one
+// multiply-add per address instead of 64-bit index arithmetic).
+template <class S, int KIND, typename I>
+__global__ void __launch_bounds__(kBlock) k_step_dev_pull(const typename S::elem* __restrict__ src,
+                                                         typename S::elem* __restrict__ dst, int nx, int ny,
+                                                         int ld, int ftiles, ShiftParamsF p) {
+  const int x = blockIdx.x / ftiles;
+  const int y = (blockIdx.x - x * ftiles) * blockDim.x + threadIdx.x;
+  if (y >= ny) return;
+  const I L = (I)ld, P = (I)ld * (I)nx;
+  const I c0 = (I)x * L, cm = (I)wrap_m(x, nx) * L, cp = (I)wrap_p(x, nx) * L;
+  const I y0 = (I)y, ym = (I)wrap_m(y, ny), yp = (I)wrap_p(y, ny);
+  float h[9];
+  h[0] = S::load(src, c0 + y0);
+  h[1] = S::load(src, P + cm + y0);
+  h[2] = S::load(src, 2 * P + c0 + ym);
+  h[3] = S::load(src, 3 * P + cp + y0);
+  h[4] = S::load(src, 4 * P + c0 + yp);
+  h[5] = S::load(src, 5 * P + cm + ym);
+  h[6] = S::load(src, 6 * P + cp + ym);
+  h[7] = S::load(src, 7 * P + cp + yp);
+  h[8] = S::load(src, 8 * P + cm + yp);
+  if (KIND == K_TRT) coll_trt_shift<float>(h, p.a, p.b, p.c);
+  else if (KIND == K_RR) coll_rr_shift<float>(h, p.a, p.b, p.c);
+  else coll_bgk_shift<float>(h, p.a);
+  const I o = c0 + y0;
+#pragma unroll
+  for (int q = 0; q < 9; q++) S::store(dst, (I)q * P + o, h[q]);
+}
+
 template <class S>
 __global__ void __launch_bounds__(kBlock) k_stream_dev(const typename S::elem* __restrict__ src,
                                                       typename S::elem* __restrict__ dst, int nx, int ny,
@@ -107,11 +150,33 @@ cudaError_t launch_collide_dev(int kind, const Sweep& s, const CollParams& p) {
   return cudaGetLastError();
 }
 
+template <class S, typename I>
+cudaError_t launch_pull_dev(int kind, const Sweep& s, const CollParams& cp) {
+  const int ft = tiles(s.ny);
+  const long long blocks = (long long)ft * s.nx;
+  if (blocks <= 0 || blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+  typedef typename S::elem E;
+  const E* a = static_cast<const E*>(s.src);
+  E* b = static_cast<E*>(s.dst);
+  const ShiftParamsF p = shift_params(kind, cp);
+  const unsigned nb = (unsigned)blocks;
+  switch (kind) {
+    case K_BGK: k_step_dev_pull<S, K_BGK, I><<<nb, kBlock, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft, p); break;
+    case K_TRT: k_step_dev_pull<S, K_TRT, I><<<nb, kBlock, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft, p); break;
+    case K_RR: k_step_dev_pull<S, K_RR, I><<<nb, kBlock, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft, p); break;
+    default: return cudaErrorNotSupported;
+  }
+  return cudaGetLastError();
+}
+
 }  // namespace
 
 cudaError_t step_pull_dev(int storage, int kind, const Sweep& s, const CollParams& p) {
-  if (storage == ST_F32DEV) return launch_dev<YFast, StoreF32Dev, false>(kind, s, p);
-  if (storage == ST_F16DEV) return launch_dev<YFast, StoreF16Dev, false>(kind, s, p);
+  const bool small = (unsigned long long)s.ld * (unsigned long long)s.nx * 9ull < (1ull << 32);
+  if (storage == ST_F32DEV)
+    return small ? launch_pull_dev<StoreF32Dev, uint32_t>(kind, s, p) : launch_pull_dev<StoreF32Dev, size_t>(kind, s, p);
+  if (storage == ST_F16DEV)
+    return small ? launch_pull_dev<StoreF16Dev, uint32_t>(kind, s, p) : launch_pull_dev<StoreF16Dev, size_t>(kind, s, p);
   return cudaErrorInvalidValue;
 }
 

@@ -41,23 +41,32 @@ __global__ void __launch_bounds__(kBlock) k_step_dev_df(const typename S::elem* 
   for (int q = 0; q < 9; q++) S::store(dst, YFast::off(x, y, q, nx, ny, ld), h[q].hi + h[q].lo);
 }
 
-// Deviation storage, BGK with the compensated binary32 operator.
-template <class S>
+// Deviation storage, BGK with the compensated binary32 operator.  I: offset
+// type (32-bit when the lattice has fewer than 2^32 elements).
+template <class S, typename I>
 __global__ void __launch_bounds__(kBlock) k_step_dev_comp(const typename S::elem* __restrict__ src,
                                                          typename S::elem* __restrict__ dst, int nx, int ny, int ld,
                                                          int ftiles, df::DevParams p) {
   const int x = blockIdx.x / ftiles;
   const int y = (blockIdx.x - x * ftiles) * blockDim.x + threadIdx.x;
   if (y >= ny) return;
+  const I L = (I)ld, P = (I)ld * (I)nx;
+  const I c0 = (I)x * L, cm = (I)wrap_m(x, nx) * L, cp = (I)wrap_p(x, nx) * L;
+  const I y0 = (I)y, ym = (I)wrap_m(y, ny), yp = (I)wrap_p(y, ny);
   float h[9];
-#pragma unroll
-  for (int q = 0; q < 9; q++) {
-    const int sx = wrap_add(x, -cx_of(q), nx), sy = wrap_add(y, -cy_of(q), ny);
-    h[q] = S::load(src, YFast::off(sx, sy, q, nx, ny, ld));
-  }
+  h[0] = S::load(src, c0 + y0);
+  h[1] = S::load(src, P + cm + y0);
+  h[2] = S::load(src, 2 * P + c0 + ym);
+  h[3] = S::load(src, 3 * P + cp + y0);
+  h[4] = S::load(src, 4 * P + c0 + yp);
+  h[5] = S::load(src, 5 * P + cm + ym);
+  h[6] = S::load(src, 6 * P + cp + ym);
+  h[7] = S::load(src, 7 * P + cp + yp);
+  h[8] = S::load(src, 8 * P + cm + yp);
   df::bgk_dev_comp(h, p);
+  const I o = c0 + y0;
 #pragma unroll
-  for (int q = 0; q < 9; q++) S::store(dst, YFast::off(x, y, q, nx, ny, ld), h[q]);
+  for (int q = 0; q < 9; q++) S::store(dst, (I)q * P + o, h[q]);
 }
 
 // Deviation storage, collision evaluated in binary64 on h (any kind but BGKI).
@@ -304,14 +313,20 @@ cudaError_t step_pull_dev_hi(int storage, int math, int kind, const Sweep& s, co
       p.omw3[i] = split_const(3.0 * cp.omega * w[i]);
       p.omwf[i] = (float)(cp.omega * w[i]);
     }
-    if (storage == ST_F32DEV)
-      k_step_dev_comp<StoreF32Dev><<<nb, kBlock, 0, s.stream>>>(static_cast<const float*>(s.src),
-                                                                static_cast<float*>(s.dst), s.nx, s.ny, s.ld, ft, p);
-    else if (storage == ST_F16DEV)
-      k_step_dev_comp<StoreF16Dev><<<nb, kBlock, 0, s.stream>>>(static_cast<const __half*>(s.src),
-                                                                static_cast<__half*>(s.dst), s.nx, s.ny, s.ld, ft, p);
-    else
+    const bool small = (unsigned long long)s.ld * (unsigned long long)s.nx * 9ull < (1ull << 32);
+    if (storage == ST_F32DEV) {
+      const float* a = static_cast<const float*>(s.src);
+      float* b = static_cast<float*>(s.dst);
+      if (small) k_step_dev_comp<StoreF32Dev, uint32_t><<<nb, kBlock, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft, p);
+      else k_step_dev_comp<StoreF32Dev, size_t><<<nb, kBlock, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft, p);
+    } else if (storage == ST_F16DEV) {
+      const __half* a = static_cast<const __half*>(s.src);
+      __half* b = static_cast<__half*>(s.dst);
+      if (small) k_step_dev_comp<StoreF16Dev, uint32_t><<<nb, kBlock, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft, p);
+      else k_step_dev_comp<StoreF16Dev, size_t><<<nb, kBlock, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft, p);
+    } else {
       return cudaErrorInvalidValue;
+    }
     return cudaGetLastError();
   }
   if (math == 3) {  // double-float
