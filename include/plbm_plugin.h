@@ -32,7 +32,9 @@ typedef struct plbm_plugin_params {
     int kind;          /* PLBM_BGK | PLBM_TRT | PLBM_RR                    */
     int storage;       /* PLBM_F64 | PLBM_F32DEV | PLBM_F16DEV             */
     double trt_magic;  /* TRT magic parameter (Lambda)                     */
-    int math;          /* version 2: PLBM_MATH_FMA | PLBM_MATH_STRICT      */
+    int math;          /* version 2: PLBM_MATH_FMA | PLBM_MATH_STRICT |
+                          PLBM_MATH_HYBRID (PLBM_F64: the hybrid binary64
+                          arithmetic on the shifted populations)           */
 } plbm_plugin_params;
 
 /* siminit -- sim/lbm.h:13-15, sim/sim_slbm.F90:158-172 */

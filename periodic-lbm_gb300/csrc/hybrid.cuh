@@ -202,6 +202,67 @@ DF_HD double fixed_to_double_fast(int64_t T) {
   return fixed_to_double_slow(T);
 }
 
+// ---- shifted populations h = f - w (the plugin path) -------------------------
+// With h in place of f the exact sums give DH = sum h = rho - 1 and the same
+// J; every linear bracket keeps its form with DH in place of R (the w terms
+// cancel), and rho = 1 + DH where the nonlinear terms need it.  The range
+// limits apply to |h|.
+
+// binary64 h (either sign, |h| < 2^(EMAX-1022)) -> int64 fixed point, scale
+// 2^59, truncating toward zero: one 64-bit shift; the value of to_fixed_lim.
+template <int EMAX>
+DF_HD int64_t to_fixed_signed(double d, bool& bad) {
+  const uint64_t u = df::d2u(d);
+  const int e = (int)((u >> 52) & 0x7FF);
+  if (e > EMAX) {
+    bad = true;
+    return 0;
+  }
+  const uint64_t m = (u & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
+  const int sh = e - 1016;  // value * 2^59 = m * 2^(e - 1016)
+  const uint64_t F = sh >= 0 ? (m << sh) : (-sh < 64 ? (m >> -sh) : 0ull);
+  return (u >> 63) ? -(int64_t)F : (int64_t)F;
+}
+
+// int64 fixed point (any value) -> binary64 with round-half-up, branch-free
+// apart from zero.
+DF_HD double fixed_to_double_any(int64_t T) {
+  if (T == 0) return 0.0;
+  const uint64_t neg = (uint64_t)T >> 63;
+  const uint64_t a = neg ? (uint64_t)(-T) : (uint64_t)T;
+  const int lz = clz64(a);
+  const uint64_t n = a << lz;                      // bit 63 set
+  const uint64_t m = (n >> 11) + ((n >> 10) & 1);  // <= 2^53; 2^53 carries into the exponent
+  const uint64_t ex = (uint64_t)(1086 - lz - kScale);
+  return df::u2d((neg << 63) | ((ex << 52) + (m - (1ull << 52))));
+}
+
+constexpr int64_t kOne = (int64_t)1 << kScale;  // 1.0 in fixed point
+
+template <bool SHIFTED>
+DF_HD void load_cell(const double (&f)[9], int64_t (&F)[9], bool& bad) {
+  if constexpr (SHIFTED) {
+    F[0] = to_fixed_signed<kExpRest>(f[0], bad);
+    F[1] = to_fixed_signed<kExpAxis>(f[1], bad);
+    F[2] = to_fixed_signed<kExpAxis>(f[2], bad);
+    F[3] = to_fixed_signed<kExpAxis>(f[3], bad);
+    F[4] = to_fixed_signed<kExpAxis>(f[4], bad);
+    F[5] = to_fixed_signed<kExpDiag>(f[5], bad);
+    F[6] = to_fixed_signed<kExpDiag>(f[6], bad);
+    F[7] = to_fixed_signed<kExpDiag>(f[7], bad);
+    F[8] = to_fixed_signed<kExpDiag>(f[8], bad);
+  } else {
+    load_fixed(f, F, bad);
+  }
+}
+
+// Linear terms T (R + 3 c.J, R, DH + 3 c.J, ...) to binary64.
+template <bool SHIFTED>
+DF_HD double lin_to_double(int64_t T) {
+  if constexpr (SHIFTED) return fixed_to_double_any(T);
+  else return fixed_to_double_fast(T);
+}
+
 struct Params {
   double omb;     // 1 - omega
   double omw[3];  // omega * w for w0, ws, wd
@@ -210,15 +271,17 @@ struct Params {
 
 // BGK in the hybrid arithmetic (in place).  On `bad` the populations are
 // left in an unspecified state: the caller evaluates the cell another way.
+// SHIFTED: f holds h = f - w (sim/sim.F90:445-499 semantics, rho = sum h + 1).
+template <bool SHIFTED = false>
 DF_HD void bgk_fast(double (&f)[9], const Params& p, bool& bad) {
   int64_t F[9];
-  load_fixed(f, F, bad);
+  load_cell<SHIFTED>(f, F, bad);
   const int64_t R = (((F[5] + F[7]) + (F[6] + F[8])) + ((F[1] + F[3]) + (F[2] + F[4]))) + F[0];
   const int64_t d57 = F[5] - F[7], d86 = F[8] - F[6];
   const int64_t JX = (d57 + d86) + (F[1] - F[3]);
   const int64_t JY = (d57 - d86) + (F[2] - F[4]);
-  const double Rd = fixed_to_double_fast(R);
-  const df64 rho = df::from_double(Rd);
+  const double Rd = lin_to_double<SHIFTED>(R);
+  const df64 rho = df::from_double(SHIFTED ? fixed_to_double_fast(R + kOne) : Rd);
   const df64 inv = df::recip(rho);
   const df64 ux = df::mul(fixed_to_df(JX), inv), uy = df::mul(fixed_to_df(JY), inv);
   const df64 u2_15 = df::mul_f(df::add(df::sqr(ux), df::sqr(uy)), 1.5f);
@@ -231,8 +294,8 @@ DF_HD void bgk_fast(double (&f)[9], const Params& p, bool& bad) {
     const double c = df::pack_double(                                                       \
         df::mul(p.omw_df[WI], df::mul(rho, df::sub(df::mul_f(df::sqr(CU), 4.5f), u2_15))));  \
     const int64_t cj3 = 3 * (CJ);                                                           \
-    f[QP] = fma_d(p.omw[WI], fixed_to_double_fast(R + cj3), fma_d(p.omb, f[QP], c));        \
-    f[QM] = fma_d(p.omw[WI], fixed_to_double_fast(R - cj3), fma_d(p.omb, f[QM], c));        \
+    f[QP] = fma_d(p.omw[WI], lin_to_double<SHIFTED>(R + cj3), fma_d(p.omb, f[QP], c));      \
+    f[QM] = fma_d(p.omw[WI], lin_to_double<SHIFTED>(R - cj3), fma_d(p.omb, f[QM], c));      \
   }
   PLBM_HY_PAIR(1, 3, ux, JX, 1)
   PLBM_HY_PAIR(2, 4, uy, JY, 1)
@@ -252,10 +315,11 @@ struct TrtParams {
   df64 c1[2];      // les 2w 1.5: coefficient of |j|^2 in sym
 };
 
-// TRT in the hybrid arithmetic (in place); `bad` as for bgk_fast.
+// TRT in the hybrid arithmetic (in place); `bad` and SHIFTED as for bgk_fast.
+template <bool SHIFTED = false>
 DF_HD void trt_fast(double (&f)[9], const TrtParams& p, bool& bad) {
   int64_t F[9];
-  load_fixed(f, F, bad);
+  load_cell<SHIFTED>(f, F, bad);
   const int64_t R = (((F[5] + F[7]) + (F[6] + F[8])) + ((F[1] + F[3]) + (F[2] + F[4]))) + F[0];
   const int64_t d57 = F[5] - F[7], d86 = F[8] - F[6];
   const int64_t JX = (d57 + d86) + (F[1] - F[3]);
@@ -264,7 +328,7 @@ DF_HD void trt_fast(double (&f)[9], const TrtParams& p, bool& bad) {
   const df64 j2 = df::add(df::sqr(jx), df::sqr(jy));
   {
     const double c0 = df::pack_double(df::mul(p.nl0, j2));
-    f[0] = fma_d(p.omb, f[0], fma_d(p.le_t0, fixed_to_double_fast(R), c0));
+    f[0] = fma_d(p.omb, f[0], fma_d(p.le_t0, lin_to_double<SHIFTED>(R), c0));
   }
   const df64 c1j2[2] = {df::mul(p.c1[0], j2), df::mul(p.c1[1], j2)};
   // MS, MD: the exact brackets of the pair; VDF = c_p.j
@@ -316,10 +380,11 @@ struct RrParams {
 //   a_xy = Pxy - jx uy,
 // Pxx = sum cx^2 F, Pyy = sum cy^2 F, Pxy = sum cx cy F.  One binary64 FMA per
 // population: f'_q = fma(w_q, T_q, w_q (rho NL_q + (1 - omega) H_q)).
+template <bool SHIFTED = false>
 DF_HD void rr_fast(double (&f)[9], const RrParams& p, bool& bad) {
   using namespace df;
   int64_t F[9];
-  load_fixed(f, F, bad);
+  load_cell<SHIFTED>(f, F, bad);
   const int64_t s57 = F[5] + F[7], s68 = F[6] + F[8];
   const int64_t sd = s57 + s68;
   const int64_t R = ((s57 + s68) + ((F[1] + F[3]) + (F[2] + F[4]))) + F[0];
@@ -329,8 +394,8 @@ DF_HD void rr_fast(double (&f)[9], const RrParams& p, bool& bad) {
   const int64_t PXX3 = 3 * ((F[1] + F[3]) + sd) - R;
   const int64_t PYY3 = 3 * ((F[2] + F[4]) + sd) - R;
   const int64_t PXY = s57 - s68;
-  const double Rd = fixed_to_double_fast(R);
-  const df64 rho = from_double(Rd);
+  const double Rd = lin_to_double<SHIFTED>(R);
+  const df64 rho = from_double(SHIFTED ? fixed_to_double_fast(R + kOne) : Rd);
   const df64 inv = recip(rho);
   const df64 jx = fixed_to_df(JX), jy = fixed_to_df(JY);
   const df64 ux = mul(jx, inv), uy = mul(jy, inv);
@@ -364,8 +429,8 @@ DF_HD void rr_fast(double (&f)[9], const RrParams& p, bool& bad) {
     const df64 X = add(mul(rho, (A)), mul(p.omb, (C)));                                       \
     const df64 Y = add(mul(rho, (B)), mul(p.omb, (D)));                                       \
     const int64_t cj3 = 3 * (CJ);                                                             \
-    f[QP] = fma_d(p.w[WI], fixed_to_double_fast(R + cj3), pack_double(mul(p.wdf[WI], add(X, Y)))); \
-    f[QM] = fma_d(p.w[WI], fixed_to_double_fast(R - cj3), pack_double(mul(p.wdf[WI], sub(X, Y)))); \
+    f[QP] = fma_d(p.w[WI], lin_to_double<SHIFTED>(R + cj3), pack_double(mul(p.wdf[WI], add(X, Y)))); \
+    f[QM] = fma_d(p.w[WI], lin_to_double<SHIFTED>(R - cj3), pack_double(mul(p.wdf[WI], sub(X, Y)))); \
   }
   PLBM_HY_RR_PAIR(1, 3, add(nls, mul_f(uxx, 4.5f)), mul_f(uyyx, -4.5f), add(is, mul_f(axx, 4.5f)),
                   mul_f(ayyx, -4.5f), JX, 1)

@@ -44,6 +44,9 @@ PLBM_DECLARE_F64(strict)
 
 // binary64 storage, hybrid arithmetic (hybrid.cuh), YFast pull, BGK, TRT and RR
 cudaError_t step_pull_df64(int kind, const Sweep& s, const CollParams& p);
+// The plugin step (shifted binary64, x-fastest, collide then push) in the
+// hybrid arithmetic (BGK, TRT, RR).
+cudaError_t step_push_hybrid(int kind, const Sweep& s, const CollParams& p);
 // A finite-volume / finite-difference streaming scheme (stencil form) fused
 // with the hybrid collision (BGK, TRT, RR).
 cudaError_t step_scheme_hybrid(int scheme, int kind, const Sweep& s, double dt, const CollParams& p);

@@ -73,6 +73,7 @@ int do_steps(PluginSim* s, double omega, int nsteps) {
     cudaError_t e;
     if (s->storage != PLBM_F64) e = step_push_dev(s->storage, s->kind, sw, p);
     else if (s->math == PLBM_MATH_STRICT) e = strict::step_push_shift_f64(s->kind, sw, p);
+    else if (s->math == PLBM_MATH_HYBRID) e = step_push_hybrid(s->kind, sw, p);
     else e = fma::step_push_shift_f64(s->kind, sw, p);
     if (e != cudaSuccess) return s->status = cuda_fail(e, "plugin step kernel");
     s->cur = 1 - s->cur;  // move_alloc swap, sim/sim_slbm.F90:114-119
@@ -121,8 +122,12 @@ extern "C" void* c_plbmgpu_init(int nx, int ny, double dt, const double* rho, co
     fail(PLBM_E_INVALID, "plugin storage %d", storage);
     return nullptr;
   }
-  if (math != PLBM_MATH_FMA && math != PLBM_MATH_STRICT) {
-    fail(PLBM_E_INVALID, "plugin math %d (FMA or STRICT)", math);
+  if (math != PLBM_MATH_FMA && math != PLBM_MATH_STRICT && math != PLBM_MATH_HYBRID) {
+    fail(PLBM_E_INVALID, "plugin math %d (FMA, STRICT or HYBRID)", math);
+    return nullptr;
+  }
+  if (math == PLBM_MATH_HYBRID && storage != PLBM_F64) {
+    fail(PLBM_E_INVALID, "plugin math HYBRID needs PLBM_F64 storage");
     return nullptr;
   }
   int ndev = 0;

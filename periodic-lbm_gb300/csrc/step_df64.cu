@@ -198,6 +198,57 @@ __global__ void __launch_bounds__(kBlock) k_step_scheme_hybrid(const double* __r
   for (int q = 0; q < 9; q++) dst[YFast::off(x, y, q, nx, ny, ld)] = f[q];
 }
 
+// The plugin step (sim/sim.F90:404-505 + :568-624) in the hybrid arithmetic:
+// shifted binary64 populations h = f - w in the x-fastest layout, collide at
+// the cell, push along c_q.  Out-of-range cells take the shifted binary64
+// operator of the FMA plugin kernel (out of line).
+template <int KIND>
+__device__ __noinline__ void push_fallback_cell(const double* __restrict__ src, double* __restrict__ dst, int x,
+                                                int y, int nx, int ny, int ld, const CollParams& p) {
+  double f[9];
+#pragma unroll
+  for (int q = 0; q < 9; q++) f[q] = src[XFast::off(x, y, q, nx, ny, ld)];
+  collide_shift<KIND, double>(f, p);
+#pragma unroll
+  for (int q = 0; q < 9; q++) dst[XFast::off(wrap_add(x, cx_of(q), nx), wrap_add(y, cy_of(q), ny), q, nx, ny, ld)] = f[q];
+  g_hybrid_range_flag = 1;
+}
+
+template <typename I, int KIND>
+__global__ void __launch_bounds__(kBlock, hybrid_min_blocks(KIND)) k_push_hybrid(const double* __restrict__ src,
+                                                                                double* __restrict__ dst, int nx,
+                                                                                int ny, int ld, int ftiles,
+                                                                                HybridArgs a) {
+  const int y = blockIdx.x / ftiles;
+  const int x = (blockIdx.x - y * ftiles) * blockDim.x + threadIdx.x;
+  if (x >= nx) return;
+  const I L = (I)ld, P = (I)ld * (I)ny;
+  const I o = (I)y * L + (I)x;
+  double f[9];
+#pragma unroll
+  for (int q = 0; q < 9; q++) f[q] = __ldg(src + ((I)q * P + o));
+  bool bad = false;
+  if (KIND == K_TRT) hy::trt_fast<true>(f, a.trt, bad);
+  else if (KIND == K_RR) hy::rr_fast<true>(f, a.rr, bad);
+  else hy::bgk_fast<true>(f, a.bgk, bad);
+  if (bad) {
+    push_fallback_cell<KIND>(src, dst, x, y, nx, ny, ld, a.ref);
+    return;
+  }
+  const I xm = (I)wrap_m(x, nx), xp = (I)wrap_p(x, nx), x0 = (I)x;
+  const I rm = (I)wrap_m(y, ny) * L, rp = (I)wrap_p(y, ny) * L, r0 = (I)y * L;
+  // push: f_q goes to (x + cx_q, y + cy_q)
+  dst[r0 + x0] = f[0];
+  dst[P + r0 + xp] = f[1];
+  dst[2 * P + rp + x0] = f[2];
+  dst[3 * P + r0 + xm] = f[3];
+  dst[4 * P + rm + x0] = f[4];
+  dst[5 * P + rp + xp] = f[5];
+  dst[6 * P + rp + xm] = f[6];
+  dst[7 * P + rm + xm] = f[7];
+  dst[8 * P + rm + xp] = f[8];
+}
+
 template <int KIND>
 cudaError_t launch_hybrid(const Sweep& s, unsigned blocks, int ft, const HybridArgs& a) {
   const double* src = static_cast<const double*>(s.src);
@@ -266,6 +317,35 @@ cudaError_t step_pull_df64(int kind, const Sweep& s, const CollParams& cp) {
   if (kind == K_TRT) return launch_hybrid<K_TRT>(s, (unsigned)blocks, ft, a);
   if (kind == K_RR) return launch_hybrid<K_RR>(s, (unsigned)blocks, ft, a);
   return launch_hybrid<K_BGK>(s, (unsigned)blocks, ft, a);
+}
+
+cudaError_t step_push_hybrid(int kind, const Sweep& s, const CollParams& cp) {
+  if (kind != K_BGK && kind != K_TRT && kind != K_RR) return cudaErrorNotSupported;
+  const int ft = (s.nx + kBlock - 1) / kBlock;
+  const long long blocks = (long long)ft * s.ny;
+  if (blocks <= 0 || blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+  HybridArgs a;
+  a.bgk = hybrid_params(cp.omega);
+  a.trt = hybrid_trt_params(cp);
+  a.rr = hybrid_rr_params(cp);
+  a.ref = cp;
+  const double* src = static_cast<const double*>(s.src);
+  double* dst = static_cast<double*>(s.dst);
+  const unsigned nb = (unsigned)blocks;
+  const bool small = (unsigned long long)s.ld * (unsigned long long)s.ny * 9ull < (1ull << 32);
+#define PLBM_PUSH_HY(I)                                                                                      \
+  switch (kind) {                                                                                            \
+    case K_BGK: k_push_hybrid<I, K_BGK><<<nb, kBlock, 0, s.stream>>>(src, dst, s.nx, s.ny, s.ld, ft, a); break; \
+    case K_TRT: k_push_hybrid<I, K_TRT><<<nb, kBlock, 0, s.stream>>>(src, dst, s.nx, s.ny, s.ld, ft, a); break; \
+    default: k_push_hybrid<I, K_RR><<<nb, kBlock, 0, s.stream>>>(src, dst, s.nx, s.ny, s.ld, ft, a); break;     \
+  }
+  if (small) {
+    PLBM_PUSH_HY(uint32_t)
+  } else {
+    PLBM_PUSH_HY(size_t)
+  }
+#undef PLBM_PUSH_HY
+  return cudaGetLastError();
 }
 
 cudaError_t step_scheme_hybrid(int scheme, int kind, const Sweep& s, double dt, const CollParams& cp) {

@@ -83,7 +83,7 @@ def run_plugin(args) -> dict:
     case = TGVStudy((n, n), umax=0.05, k=(k, k), nu=0.02)
     p0, u0 = case.solution(0.0)
     sim = SimPlugin()
-    sim.init((n, n), 1.0, p0, u0, params=make_params(kind=args.kind, storage=args.storage))
+    sim.init((n, n), 1.0, p0, u0, params=make_params(kind=args.kind, storage=args.storage, math=args.math))
     omega = 1.0 / (3 * 0.02 + 0.5)
     sim.steps(omega, args.warmup)
     sim.synchronize()
@@ -93,7 +93,8 @@ def run_plugin(args) -> dict:
     sim.synchronize()
     ms = (time.perf_counter() - t0) * 1e3 / max(args.steps, 1)
     sim.free()
-    return {"workload": "plugin", "n": n, "kind": args.kind, "storage": args.storage, "ms_per_step": ms,
+    return {"workload": "plugin", "n": n, "kind": args.kind, "storage": args.storage, "math": args.math,
+            "ms_per_step": ms,
             "mlups": n * n / (ms * 1e-3) / 1e6}
 
 

@@ -151,3 +151,46 @@ def test_studies_perfsweep_on_gpu_plugin(gpu_lib):
     from plbm.plugin import SimPlugin
     out = studies.perfsweep(SimPlugin(), 256, 1024, step=256, tsteps=50, dt=1.0)
     assert out["grids"] == [256, 512, 768] and min(out["mlups"]) > 0
+
+
+def test_plugin_hybrid_bgk_within_1e12(gpu_lib):
+    """PLBM_MATH_HYBRID on the plugin's shifted binary64 populations against
+    the oracle's restatement of sim/sim_slbm.F90 + sim/sim.F90."""
+    from plbm.plugin import SimPlugin, make_params
+    nx, ny = 96, 80
+    p, u = tgv_fields(nx, ny)
+    sim = SimPlugin()
+    sim.init((nx, ny), 1.0, p, u, params=make_params(math="hybrid"))
+    sim.steps(1.3, 300)
+    rho, uu = sim.vars()
+    sim.free()
+    r, ux, uy = oracle_run(p, u, 1.3, 300)
+    rel = lambda a, b: np.max(np.abs(a - b)) / np.max(np.abs(b))  # noqa: E731
+    assert rel(rho, r) <= 1e-12
+    assert rel(uu[:, :, 0], ux) <= 1e-12 and rel(uu[:, :, 1], uy) <= 1e-12
+
+
+@pytest.mark.parametrize("kind", ["trt", "rr"])
+def test_plugin_hybrid_other_collisions_match_fma(gpu_lib, kind):
+    from plbm.plugin import SimPlugin, make_params
+    nx, ny = 64, 48
+    p, u = tgv_fields(nx, ny)
+    out = []
+    for m in ("fma", "hybrid"):
+        sim = SimPlugin()
+        sim.init((nx, ny), 1.0, p, u, params=make_params(kind=kind, math=m))
+        sim.steps(1.6, 200)
+        out.append(sim.vars())
+        sim.free()
+    (r0, u0), (r1, u1) = out
+    assert np.max(np.abs(r1 - r0)) <= 1e-12 * np.max(np.abs(r0))
+    assert np.max(np.abs(u1 - u0)) <= 1e-12 * np.max(np.abs(u0))
+
+
+def test_plugin_hybrid_needs_f64(gpu_lib):
+    from plbm import PlbmError
+    from plbm.plugin import SimPlugin, make_params
+    p, u = tgv_fields(16, 16)
+    sim = SimPlugin()
+    with pytest.raises(PlbmError):
+        sim.init((16, 16), 1.0, p, u, params=make_params(storage="f32dev", math="hybrid"))
