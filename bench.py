@@ -212,6 +212,48 @@ def time_grid_steps(torch, n, storage, kind, math_mode, omega, steps, warmup, fi
     return ms / steps
 
 
+def time_scheme_steps(torch, n, scheme, math_mode, steps, warmup, fields):
+    """Device MLUPS of perform_lbm_step with a finite-volume / finite-difference
+    streaming scheme (dt = 0.3, nu = 0.05) and BGK."""
+    from plbm import LatticeGrid
+    stream = torch.cuda.Stream()
+    g = LatticeGrid(n, n, collision="bgk", math=math_mode, streaming=scheme)
+    g.set_stream(stream.cuda_stream)
+    g.set_properties(0.05, 0.3)
+    g.set_pdf_to_equilibrium(*fields)
+    g.perform_lbm_step(warmup)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    g.perform_lbm_step(steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    g.close()
+    return ms / steps
+
+
+def time_plugin_steps(n, math_mode, steps, warmup):
+    """MLUPS of the sim/ plugin ABI (c_plbmgpu_*) at n^2, binary64 BGK, host
+    clock around c_plbmgpu_steps + c_plbmgpu_synchronize."""
+    from plbm.plugin import SimPlugin, make_params
+    from plbm.studies import TGVStudy
+    k = 2 * math.pi / n
+    p0, u0 = TGVStudy((n, n), umax=0.05, k=(k, k), nu=0.02).solution(0.0)
+    sim = SimPlugin()
+    sim.init((n, n), 1.0, p0, u0, params=make_params(math=math_mode))
+    del p0, u0
+    omega = 1.0 / (3 * 0.02 + 0.5)
+    sim.steps(omega, warmup)
+    sim.synchronize()
+    t0 = time.perf_counter()
+    sim.steps(omega, steps)
+    sim.synchronize()
+    dt = time.perf_counter() - t0
+    sim.free()
+    return dt * 1e3 / steps
+
+
 def variant_entry(n, storage, ms_step, peak):
     mlups = n * n / (ms_step * 1e-3) / 1e6
     gbs = mlups * 1e6 * BYTES_PER_CELL[storage] / 1e9
@@ -455,6 +497,17 @@ def main() -> None:
                 e = variant_entry(n, "f64", time_grid_steps(torch, n, "f64", other, mm, omega, 20, 3, fields), peak)
                 e["workload"] = f"{n}^2 {other.upper()} binary64, {mm} arithmetic, same state and tau"
                 var[f"fp64_{other}_{mm}"] = e
+        for scheme in ("fdm_bardow", "fdm_sofonea"):
+            for mm in ("hybrid", "strict"):
+                e = variant_entry(n, "f64", time_scheme_steps(torch, n, scheme, mm, 10, 2, fields), peak)
+                e["workload"] = (f"{n}^2 BGK with grid%streaming => stream_{scheme}, dt=0.3 nu=0.05, "
+                                 + ("fused stencil + hybrid collision" if mm == "hybrid" else
+                                    "reference expressions, two passes"))
+                var[f"scheme_{scheme}_{mm}"] = e
+        for mm in ("hybrid", "fma"):
+            e = variant_entry(n, "f64", time_plugin_steps(n, mm, 20, 3), peak)
+            e["workload"] = f"{n}^2 sim/ plugin ABI (c_plbmgpu_*), binary64 BGK, {mm} arithmetic, host clock"
+            var[f"plugin_f64_{mm}"] = e
         var["fp32dev"] = variant_entry(n, "f32dev", time_grid_steps(torch, n, "f32dev", args.kind, "fma", omega, 50, 3,
                                                                    fields), peak)
         if args.kind == "bgk":
