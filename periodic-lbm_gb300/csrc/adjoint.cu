@@ -139,8 +139,11 @@ __global__ void __launch_bounds__(kBlock) k_adj_final(const void* __restrict__ f
 }
 
 // One reverse step: lambda_n from lambda_{n+1} and f_n; adds this step's
-// dL/domega to the block's binary64 slot.
-template <int ST>
+// dL/domega to the block's binary64 slot.  I: offset type (32-bit when the
+// lattice has fewer than 2^32 elements).  The pull sources of the forward
+// step are also where the reverse step scatters mu_p, so one offset table
+// serves the loads of f and the stores of lambda_n.
+template <int ST, typename I>
 __global__ void __launch_bounds__(kBlock) k_adj_step(const void* __restrict__ f, const void* __restrict__ lam_in,
                                                     void* __restrict__ lam_out, double* __restrict__ dom,
                                                     typename AdjTraits<ST>::real om, int nx, int ny, int ld,
@@ -154,11 +157,16 @@ __global__ void __launch_bounds__(kBlock) k_adj_step(const void* __restrict__ f,
     const E* fe = static_cast<const E*>(f);
     const E* li = static_cast<const E*>(lam_in);
     E* lo = static_cast<E*>(lam_out);
+    const I L = (I)ld, P = (I)ld * (I)nx;
+    const I c0 = (I)x * L, cm = (I)wrap_m(x, nx) * L, cp = (I)wrap_p(x, nx) * L;
+    const I y0 = (I)y, ym = (I)wrap_m(y, ny), yp = (I)wrap_p(y, ny);
+    const I off[9] = {c0 + y0,         P + cm + y0,     2 * P + c0 + ym, 3 * P + cp + y0, 4 * P + c0 + yp,
+                      5 * P + cm + ym, 6 * P + cp + ym, 7 * P + cp + yp, 8 * P + cm + yp};
     R g[9], l[9], neq[9], rho, ux, uy;
 #pragma unroll
     for (int q = 0; q < 9; q++) {
-      g[q] = (R)__ldg(fe + YFast::off(wrap_add(x, -cx_of(q), nx), wrap_add(y, -cy_of(q), ny), q, nx, ny, ld));
-      l[q] = (R)__ldg(li + YFast::off(x, y, q, nx, ny, ld));
+      g[q] = (R)__ldg(fe + off[q]);
+      l[q] = (R)__ldg(li + ((I)q * P + c0 + y0));
     }
     cell_state<R, AdjTraits<ST>::shift>(g, rho, ux, uy, neq);
     const R u2 = ux * ux + uy * uy;
@@ -180,7 +188,7 @@ __global__ void __launch_bounds__(kBlock) k_adj_step(const void* __restrict__ f,
 #pragma unroll
     for (int p = 0; p < 9; p++) {
       const R mu = omb * l[p] + om * (A + (R)cx_of(p) * ex + (R)cy_of(p) * ey);
-      lo[YFast::off(wrap_add(x, -cx_of(p), nx), wrap_add(y, -cy_of(p), ny), p, nx, ny, ld)] = (E)mu;
+      lo[off[p]] = (E)mu;
     }
   }
   const double t = block_sum(part);
@@ -219,8 +227,14 @@ cudaError_t dispatch(int what, const AdjLaunch& a) {
     case 0: k_adj_init<ST><<<nb, kBlock, 0, a.stream>>>(a.u, const_cast<void*>(a.f), a.nx, a.ny, a.ld, ft); break;
     case 1: k_adj_final<ST><<<nb, kBlock, 0, a.stream>>>(a.f, a.g, a.out, a.lam_out, a.nx, a.ny, a.ld, ft); break;
     case 2:
-      k_adj_step<ST><<<nb, kBlock, 0, a.stream>>>(a.f, a.lam_in, a.lam_out, a.dom,
-                                                  (typename AdjTraits<ST>::real)a.omega, a.nx, a.ny, a.ld, ft);
+      if ((unsigned long long)a.ld * (unsigned long long)a.nx * 9ull < (1ull << 32))
+        k_adj_step<ST, uint32_t><<<nb, kBlock, 0, a.stream>>>(a.f, a.lam_in, a.lam_out, a.dom,
+                                                              (typename AdjTraits<ST>::real)a.omega, a.nx, a.ny,
+                                                              a.ld, ft);
+      else
+        k_adj_step<ST, size_t><<<nb, kBlock, 0, a.stream>>>(a.f, a.lam_in, a.lam_out, a.dom,
+                                                            (typename AdjTraits<ST>::real)a.omega, a.nx, a.ny, a.ld,
+                                                            ft);
       break;
     case 3: k_adj_u0<ST><<<nb, kBlock, 0, a.stream>>>(a.lam_in, a.u, a.out, a.nx, a.ny, a.ld, ft); break;
     default: return cudaErrorInvalidValue;
