@@ -254,6 +254,23 @@ def time_plugin_steps(n, math_mode, steps, warmup):
     return dt * 1e3 / steps
 
 
+# ---- replicas: one process per GPU, independent grids (no data-path collective)
+def max_over_ranks(x: float, world: int, device: str = "cuda") -> float:
+    """The slowest rank's time (the job ends when the last replica ends)."""
+    if world <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_mlups(cells_per_rank: int, steps: int, world: int, seconds_max: float) -> float:
+    """Whole-job throughput: the cell updates of all replicas over the slowest rank's time."""
+    return world * cells_per_rank * steps / seconds_max / 1e6
+
+
 def variant_entry(n, storage, ms_step, peak):
     mlups = n * n / (ms_step * 1e-3) / 1e6
     gbs = mlups * 1e6 * BYTES_PER_CELL[storage] / 1e9
@@ -423,12 +440,9 @@ def main() -> None:
     barrier()
     ms = e0.elapsed_time(e1)
     clocks = sampler.stop()
-    ms_t = torch.tensor([ms], device="cuda")
-    if world > 1:
-        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
-    ms_max = float(ms_t.item())
+    ms_max = max_over_ranks(ms, world)
     cells = n * n
-    mlups = world * cells * args.steps / (ms_max * 1e-3) / 1e6
+    mlups = job_mlups(cells, args.steps, world, ms_max * 1e-3)
 
     # ---- end to end through the C ABI with host buffers -------------------------
     # One job as the reference's time loop runs it: pinned host f(ld,nx,0:8) ->
@@ -450,10 +464,7 @@ def main() -> None:
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     barrier()
-    e2e_t = torch.tensor([e2e_s], device="cuda")
-    if world > 1:
-        dist.all_reduce(e2e_t, op=dist.ReduceOp.MAX)
-    e2e_mlups = world * cells * args.steps / float(e2e_t.item()) / 1e6
+    e2e_mlups = job_mlups(cells, args.steps, world, max_over_ranks(e2e_s, world))
     h2d = 9 * n * ld * 8
     d2h = 3 * n * n * 8
     g.close()
