@@ -285,6 +285,12 @@ int plbm_batch_run(plbm_batch_t *b, int nsteps);
 /* Capture nsteps steps into a CUDA graph for the current step parity. */
 int plbm_batch_capture(plbm_batch_t *b, int nsteps);
 int plbm_batch_launch_graph(plbm_batch_t *b);
+/* Failure injection for tests of the bounded wait: the next persistent
+ * plbm_batch_run starts with a grid-barrier arrival count that can never
+ * complete, so every CTA's wait runs out (a few seconds), the kernel returns,
+ * and plbm_batch_synchronize reports PLBM_E_TIMEOUT; the lattices are left
+ * part-stepped and the context stays usable.  Persistent schedule only. */
+int plbm_batch_inject_stall(plbm_batch_t *b);
 /* Wait; PLBM_E_TIMEOUT if a persistent run's barrier wait expired. */
 int plbm_batch_synchronize(plbm_batch_t *b);
 int plbm_batch_steps(const plbm_batch_t *b, long long *steps);

@@ -43,6 +43,7 @@ struct plbm_batch {
   plbm_batch_schedule sched{};
   int ctas = 0;
   long long steps_done = 0;
+  int stall_next = 0;           // next persistent run: unreachable barrier
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   int graph_steps[2] = {0, 0};
 };
@@ -134,6 +135,8 @@ BatchLaunch launch_of(const plbm_batch_t* b) {
 cudaError_t enqueue(plbm_batch_t* b, int nsteps) {
   if (b->sched.persistent) {
     cudaError_t e = cudaMemsetAsync(b->ctrl, 0, batch_ctrl_bytes(), b->stream);
+    if (e == cudaSuccess && b->stall_next) e = batch_arm_stall(b->ctrl, b->stream);
+    b->stall_next = 0;
     if (e != cudaSuccess) return e;
   }
   return batch_run(b->storage, launch_of(b), nsteps, (int)(b->steps_done & 1));
@@ -360,6 +363,13 @@ extern "C" int plbm_batch_launch_graph(plbm_batch_t* b) {
   CUDA_TRY(cudaSetDevice(b->device), "cudaSetDevice");
   CUDA_TRY(cudaGraphLaunch(b->graph[par], b->stream), "cudaGraphLaunch");
   b->steps_done += b->graph_steps[par];
+  return PLBM_OK;
+}
+
+extern "C" int plbm_batch_inject_stall(plbm_batch_t* b) {
+  if (!b) return fail(PLBM_E_INVALID, "NULL batch");
+  if (!b->sched.persistent) return fail(PLBM_E_INVALID, "stall injection needs the persistent schedule");
+  b->stall_next = 1;
   return PLBM_OK;
 }
 

@@ -263,6 +263,13 @@ cudaError_t batch_run(int storage, const BatchLaunch& L, int nsteps, int parity0
   return cudaErrorNotSupported;
 }
 
+cudaError_t batch_arm_stall(void* ctrl, cudaStream_t st) {
+  // arrival count far above any CTA count: the first barrier never completes
+  // and every CTA's wait runs out (kSpinLimit polls)
+  static const Ctrl stalled = {0x80000000u, 0u, 0, 0};
+  return cudaMemcpyAsync(ctrl, &stalled, sizeof stalled, cudaMemcpyHostToDevice, st);
+}
+
 cudaError_t batch_read_ctrl(const void* ctrl, int* error, int* where, cudaStream_t st) {
   Ctrl h;
   cudaError_t e = cudaMemcpyAsync(&h, ctrl, sizeof h, cudaMemcpyDeviceToHost, st);

@@ -43,5 +43,8 @@ cudaError_t batch_max_ctas(int storage, int threads, int small_index, int* per_s
 // Advance nsteps; parity0 = 0 reads lattice A first.
 cudaError_t batch_run(int storage, const BatchLaunch& L, int nsteps, int parity0);
 cudaError_t batch_read_ctrl(const void* ctrl, int* error, int* where, cudaStream_t st);
+// Make the next persistent run's first grid barrier unreachable (its waits
+// run out): the failure-path test of the bounded wait.
+cudaError_t batch_arm_stall(void* ctrl, cudaStream_t st);
 
 }  // namespace plbm

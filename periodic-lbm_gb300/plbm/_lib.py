@@ -118,6 +118,7 @@ SIGNATURES = {
     "plbm_batch_capture": (C.c_int, [_vp, C.c_int]),
     "plbm_batch_launch_graph": (C.c_int, [_vp]),
     "plbm_batch_synchronize": (C.c_int, [_vp]),
+    "plbm_batch_inject_stall": (C.c_int, [_vp]),
     "plbm_batch_steps": (C.c_int, [_vp, C.POINTER(C.c_longlong)]),
     "plbm_batch_macros": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp]),
     "plbm_batch_download": (C.c_int, [_vp, C.c_int, _vp]),

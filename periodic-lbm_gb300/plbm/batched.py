@@ -79,7 +79,7 @@ class BatchedGrids:
             self.set_math(math)
 
     def set_math(self, math: str) -> None:
-        """"fma" or, for binary64 storage, "hybrid" (BGK grids only)."""
+        """"fma" or, for binary64 storage, "hybrid" (BGK and TRT grids)."""
         check(self._lib.plbm_batch_set_math(self._h, _lib.MATHS[math]))
         self.math = math
 
@@ -139,6 +139,10 @@ class BatchedGrids:
 
     def launch_graph(self) -> None:
         check(self._lib.plbm_batch_launch_graph(self._h))
+
+    def inject_stall(self) -> None:
+        """Test hook: the next persistent run's barrier wait runs out (PLBM_E_TIMEOUT)."""
+        check(self._lib.plbm_batch_inject_stall(self._h))
 
     def synchronize(self) -> None:
         check(self._lib.plbm_batch_synchronize(self._h))

@@ -198,3 +198,27 @@ def test_batched_hybrid_rejected_for_f32dev(gpu_lib):
     with pytest.raises(PlbmError):
         b.set_math("hybrid")
     b.close()
+
+
+def test_persistent_barrier_wait_runs_out_and_the_context_survives(gpu_lib):
+    """Bounded-wait failure path: the injected run's grid barrier can never
+    complete; every CTA gives up after its bounded wait, the host reads
+    PLBM_E_TIMEOUT, and the same device then runs a batch correctly."""
+    from plbm import PlbmError
+    from plbm.batched import Schedule
+    b, _ = make_batch()
+    b.schedule = Schedule.from_dict({"threads": 128, "ctas_per_sm": 0, "persistent": 1, "ty": [32] * 5})
+    b.inject_stall()
+    b.run(3)
+    with pytest.raises(PlbmError) as e:
+        b.synchronize()
+    assert e.value.code == -5
+    b.close()
+    ok, fields = make_batch()
+    ok.schedule = Schedule.from_dict({"threads": 128, "ctas_per_sm": 0, "persistent": 1, "ty": [32] * 5})
+    ok.run(4)
+    ok.synchronize()
+    for i, (nx, ny, _, _) in enumerate(SPECS):
+        for a, c in zip(O.update_macros(ok.download(i), ny), O.update_macros(oracle_grid(i, fields, 4), ny)):
+            assert relinf(a, c) <= 1e-12
+    ok.close()
