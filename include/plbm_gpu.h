@@ -211,7 +211,9 @@ int plbm_velocity_l2_error_noalloc(int storage, int nx, int ny, int ld, const vo
  * (ny, nx, 3). */
 int plbm_output_npy(plbm_grid_t *g, const char *path);
 /* The same under the reference's name: folder/filename + step as %09d +
- * ".npy" (step < 0: no number), creating folder (mkdir -p) first. */
+ * ".npy" (step < 0: no number), creating folder (mkdir -p) first.  folder
+ * NULL or "": the working directory (the reference's concatenation would
+ * name the root directory). */
 int plbm_output_npy_step(plbm_grid_t *g, const char *folder, const char *filename, int step);
 /* Restart files: all nf lattices as binary64 f(ld,nx,0:8,nf), Fortran order
  * (deviation storage is converted).  load_state needs the same ld, nx, nf.

@@ -210,12 +210,15 @@ extern "C" int plbm_output_npy(plbm_grid_t* g, const char* path) {
 extern "C" int plbm_output_npy_step(plbm_grid_t* g, const char* folder, const char* filename, int step) {
   if (int r = check_grid(g)) return r;
   if (!filename) return fail(PLBM_E_INVALID, "NULL filename");
+  // The reference concatenates folder // '/' // filename, which without a
+  // folder names a file in the root directory; here no folder means the
+  // working directory.
   std::string full;
   if (folder && folder[0]) {
     if (int r = mkdir_p(folder)) return r;
     full = folder;
+    full += "/";
   }
-  full += "/";
   full += filename;
   if (step >= 0) {
     char num[16];

@@ -237,7 +237,7 @@ class LatticeGrid:
         check(self._lib.plbm_output_npy_step(self.handle, str(folder).encode() if folder else None,
                                              filename.encode(), int(step)))
         name = filename + (f"{step:09d}" if step >= 0 else "") + ".npy"
-        return f"{folder}/{name}" if folder else f"/{name}"
+        return f"{folder}/{name}" if folder else name
 
     def save_state(self, path) -> None:
         """All nf lattices as a Fortran-order binary64 .npy of shape (ld, nx, 9, nf)."""

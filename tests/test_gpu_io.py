@@ -91,3 +91,11 @@ def test_triple_step_state_roundtrip(gpu_lib, tmp_path):
     for b in range(3):
         assert np.array_equal(saved[:, :, :, b].T, a.download(b + 1))
     a.close()
+
+
+def test_output_npy_step_without_folder_writes_to_the_working_directory(gpu_lib, tmp_path, monkeypatch):
+    monkeypatch.chdir(tmp_path)
+    g = stepped_grid(nx=16, ny=16, steps=1)
+    name = g.output_npy_step(None, "snap", 7)
+    assert name == "snap000000007.npy" and (tmp_path / name).exists()
+    g.close()
