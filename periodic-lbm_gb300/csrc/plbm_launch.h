@@ -57,9 +57,9 @@ cudaError_t step_pull_dev(int storage, int kind, const Sweep& s, const CollParam
 cudaError_t stream_dev(int storage, const Sweep& s);
 cudaError_t collide_dev(int storage, int kind, const Sweep& s, const CollParams& p);
 cudaError_t step_push_dev(int storage, int kind, const Sweep& s, const CollParams& p);
-// Deviation storage with the collision in binary64 (math 1) or double-float
-// (math 2 compensated binary32, math 3 double-float; BGK only) arithmetic;
-// compiled in step_df64.cu.
+// Deviation storage with the collision in binary64 (math 1, BGK/TRT/RR),
+// compensated binary32 (math 2, BGK) or double-float (math 3, BGK)
+// arithmetic; compiled in step_df64.cu.
 cudaError_t step_pull_dev_hi(int storage, int math, int kind, const Sweep& s, const CollParams& p);
 
 // Field kernels (fields.cu).  layout: 0 = YFast (src/), 1 = XFast (sim/).
