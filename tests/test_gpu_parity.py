@@ -130,20 +130,21 @@ def test_hybrid_out_of_range_cells_fall_back(gpu_lib, kind, rho0):
     g.close()
 
 
-def test_hybrid_long_horizon_bench_state(gpu_lib):
-    """The bench workload's state (TGV u0 = 0.05 + N(0,1e-4^2) noise, BGK tau = 0.6)
+@pytest.mark.parametrize("kind", ["bgk", "trt", "rr"])
+def test_hybrid_long_horizon_bench_state(gpu_lib, kind):
+    """The bench workload's state (TGV u0 = 0.05 + N(0,1e-4^2) noise, tau = 0.6)
     over its full 10000-step horizon, hybrid GPU kernel against the oracle, on 96^2."""
     from plbm import LatticeGrid, cases
     n, steps, tau = 96, 10000, 0.6
     rho, ux, uy = cases.tgv_with_noise(n, u0=0.05, sigma=1e-4, seed=1234, nu=(tau - 0.5) / 3.0)
-    g = LatticeGrid(n, n, collision="bgk", math="hybrid")
+    g = LatticeGrid(n, n, collision=kind, math="hybrid")
     g.set_relaxation(1.0 / tau, 0.25)
     g.set_pdf_to_equilibrium(rho, ux, uy)
     g.perform_lbm_step(steps)
     got = g.download(g.iold)
     g.close()
     f2 = np.stack([np.zeros((9, n, n)), O.set_pdf_to_equilibrium(rho, ux, uy)])
-    iold, _ = O.perform_lbm_step(f2, n, 2, 1, O.BGK, 1.0 / tau, 0.25, steps)
+    iold, _ = O.perform_lbm_step(f2, n, 2, 1, KIND[kind], 1.0 / tau, 0.25, steps)
     for a, b in zip(O.update_macros(got, n), O.update_macros(f2[iold - 1], n)):
         assert relinf(a, b) <= TOL
 
