@@ -218,6 +218,23 @@ DF_HD uint64_t float_bits_to_double_bits(float f) {
 
 DF_HD double to_double_exactish(float f) { return u2d(float_bits_to_double_bits(f)); }
 
+// binary32 -> binary64 by bit assembly for finite values (binary32 subnormals
+// become 0); integer instructions only, no conversion on the binary64 pipe.
+DF_HD double f2d_bits(float f) {
+  const uint32_t b = f2u(f);
+  const uint32_t ex = (b >> 23) & 0xFFu;
+  const uint32_t hi = ex ? ((b & 0x80000000u) | ((ex + 896u) << 20) | ((b & 0x7FFFFFu) >> 3)) : (b & 0x80000000u);
+  const uint32_t lo = ex ? ((b & 0x7u) << 29) : 0u;
+  return u2d(((uint64_t)hi << 32) | (uint64_t)lo);
+}
+
+// hi + lo of a normalised pair as one binary64 addition of the exact binary64
+// images of hi and lo (exact whenever lo lies within 29 bits below hi's last
+// bit, as it does after renormalisation).  Costs one binary64 addition where
+// pack_double() costs ~25 integer instructions: the form for kernels whose
+// binary64 pipe has room.
+DF_HD double df_to_double(df64 a) { return f2d_bits(a.hi) + f2d_bits(a.lo); }
+
 // hi + lo rounded to binary64 without binary64 arithmetic.  For a
 // normalised pair (|lo| <= ulp(hi)/2) the 53-bit significand of hi + lo is
 // formed in a 64-bit integer: exact when lo reaches at most 29 bits below

@@ -337,8 +337,8 @@ DF_HD void trt_fast(double (&f)[9], const TrtParams& p, bool& bad) {
     const df64 sym = df::sub(df::mul(p.cs[A], fixed_to_df(MS)),                             \
                              df::sub(df::mul(p.c4[A], df::sqr(VDF)), c1j2[A]));             \
     const df64 asym = df::mul(p.cd[A], fixed_to_df(MD));                                    \
-    f[QP] = f[QP] + df::pack_double(df::neg(df::add(sym, asym)));                           \
-    f[QM] = f[QM] + df::pack_double(df::sub(asym, sym));                                    \
+    f[QP] = f[QP] + df::df_to_double(df::neg(df::add(sym, asym)));                          \
+    f[QM] = f[QM] + df::df_to_double(df::sub(asym, sym));                                   \
   }
   {
     const int64_t s = F[1] + F[3], d = F[1] - F[3];
@@ -429,8 +429,8 @@ DF_HD void rr_fast(double (&f)[9], const RrParams& p, bool& bad) {
     const df64 X = add(mul(rho, (A)), mul(p.omb, (C)));                                       \
     const df64 Y = add(mul(rho, (B)), mul(p.omb, (D)));                                       \
     const int64_t cj3 = 3 * (CJ);                                                             \
-    f[QP] = fma_d(p.w[WI], lin_to_double<SHIFTED>(R + cj3), pack_double(mul(p.wdf[WI], add(X, Y)))); \
-    f[QM] = fma_d(p.w[WI], lin_to_double<SHIFTED>(R - cj3), pack_double(mul(p.wdf[WI], sub(X, Y)))); \
+    f[QP] = fma_d(p.w[WI], lin_to_double<SHIFTED>(R + cj3), df_to_double(mul(p.wdf[WI], add(X, Y)))); \
+    f[QM] = fma_d(p.w[WI], lin_to_double<SHIFTED>(R - cj3), df_to_double(mul(p.wdf[WI], sub(X, Y)))); \
   }
   PLBM_HY_RR_PAIR(1, 3, add(nls, mul_f(uxx, 4.5f)), mul_f(uyyx, -4.5f), add(is, mul_f(axx, 4.5f)),
                   mul_f(ayyx, -4.5f), JX, 1)
