@@ -269,6 +269,10 @@ struct Params {
   df64 omw_df[3];  // the same as double-float
 };
 
+// Small terms to binary64: the TRT and RR forms add them with df_to_double
+// (bit-assembled halves and one binary64 add); BGK, whose binary64 pipe is
+// already as busy as its issue, keeps pack_double (integer only).
+
 // BGK in the hybrid arithmetic (in place).  On `bad` the populations are
 // left in an unspecified state: the caller evaluates the cell another way.
 // SHIFTED: f holds h = f - w (sim/sim.F90:445-499 semantics, rho = sum h + 1).
@@ -327,7 +331,7 @@ DF_HD void trt_fast(double (&f)[9], const TrtParams& p, bool& bad) {
   const df64 jx = fixed_to_df(JX), jy = fixed_to_df(JY);
   const df64 j2 = df::add(df::sqr(jx), df::sqr(jy));
   {
-    const double c0 = df::pack_double(df::mul(p.nl0, j2));
+    const double c0 = df::df_to_double(df::mul(p.nl0, j2));
     f[0] = fma_d(p.omb, f[0], fma_d(p.le_t0, lin_to_double<SHIFTED>(R), c0));
   }
   const df64 c1j2[2] = {df::mul(p.c1[0], j2), df::mul(p.c1[1], j2)};
@@ -421,7 +425,7 @@ DF_HD void rr_fast(double (&f)[9], const RrParams& p, bool& bad) {
     const df64 nl0 = add(base, mul_f(uxxyy, 2.25f));
     const df64 h0 = add(i0, mul_f(axxyy, 2.25f));
     const df64 b0 = add(mul(rho, nl0), mul(p.omb, h0));
-    f[0] = fma_d(p.w[0], Rd, pack_double(mul(p.wdf[0], b0)));
+    f[0] = fma_d(p.w[0], Rd, df_to_double(mul(p.wdf[0], b0)));
   }
   // pair p, m: NL = A +- B, H = C +- D, T = R +- 3 CJ
 #define PLBM_HY_RR_PAIR(QP, QM, A, B, C, D, CJ, WI)                                           \
