@@ -233,15 +233,15 @@ def time_scheme_steps(torch, n, scheme, math_mode, steps, warmup, fields):
     return ms / steps
 
 
-def time_plugin_steps(n, math_mode, steps, warmup):
-    """MLUPS of the sim/ plugin ABI (c_plbmgpu_*) at n^2, binary64 BGK, host
-    clock around c_plbmgpu_steps + c_plbmgpu_synchronize."""
+def time_plugin_steps(n, math_mode, steps, warmup, kind="bgk"):
+    """Milliseconds per step of the sim/ plugin ABI (c_plbmgpu_*) at n^2,
+    binary64 storage, host clock around c_plbmgpu_steps + c_plbmgpu_synchronize."""
     from plbm.plugin import SimPlugin, make_params
     from plbm.studies import TGVStudy
     k = 2 * math.pi / n
     p0, u0 = TGVStudy((n, n), umax=0.05, k=(k, k), nu=0.02).solution(0.0)
     sim = SimPlugin()
-    sim.init((n, n), 1.0, p0, u0, params=make_params(math=math_mode))
+    sim.init((n, n), 1.0, p0, u0, params=make_params(kind=kind, math=math_mode))
     del p0, u0
     omega = 1.0 / (3 * 0.02 + 0.5)
     sim.steps(omega, warmup)

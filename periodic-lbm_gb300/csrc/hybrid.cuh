@@ -12,11 +12,16 @@
 //   R, JX, JY = sum F_q, sum cx F_q, sum cy F_q          exact integer sums
 //
 // BGK (src/collision_bgk.F90:58-71, equilibrium src/fvm_bardow.F90:99-126):
-//   T_q      = R + 3 c_q.J                               exact integer
-//   corr_q   = omega w_q rho (4.5 (c_q.u)^2 - 1.5 u^2)   double-float, |corr| <~ 1e-3
-//   f'_q     = fma(omega w_q, T_q, fma(1 - omega, f_q, corr_q))   2 binary64 FMAs
+//   C_q      = rho (4.5 (c_q.u)^2 - 1.5 u^2)             double-float, |C| <~ 1e-2
+//   T_q      = R + 3 c_q.J + C_q                         integer (C_q's two
+//                                                        binary32 halves added exactly)
+//   f'_q     = fma(omega w_q, T_q, (1 - omega) f_q)      2 binary64 operations
 // which is f' = (1 - omega) f + omega feq with
-// feq_q = w_q (rho + 3 c.j + rho (4.5 (c.u)^2 - 1.5 u^2)), j = rho u.
+// feq_q = w_q (rho + 3 c.j + rho (4.5 (c.u)^2 - 1.5 u^2)), j = rho u.  The
+// rounded constants omega w_q are corrected for in fixed point (mass_k on the
+// rest population's R, mom_k on J in the 3 c.J terms) so that the zeroth and
+// first moments are relaxed with the factors omega sum w and
+// 3 omega sum c_x^2 w of the binary64 weights, as the reference relaxes them.
 //
 // TRT, incompressible (src/collision_trt.F90:98-152): for a pair p, m = -p
 // with v = c_p.J,
@@ -37,6 +42,8 @@
 // |R| < 5, |R + 3 c.J| < 11.5, |9 (F_p + F_m) - 2R| < 15,
 // |18 (F_p + F_m) - R| < 13, |3 (F_p - F_m) - 2V| < 3, |6 (F_p - F_m) - V| < 4
 // (in units of 2^59; each bound is the sum over q of |coefficient| x limit).
+// BGK's folded term C_q must also stay below 2 (|T_q| < 13.5), checked once
+// per cell through |C_q| <= 6 rho (1.5 |u|^2).
 // A cell with a population outside the limits reports `bad`; the kernels
 // then evaluate that cell with the binary64 operator instead.
 #pragma once
@@ -263,15 +270,60 @@ DF_HD double lin_to_double(int64_t T) {
   else return fixed_to_double_fast(T);
 }
 
+// A binary32 value in the fixed point of scale 2^59, truncated toward zero
+// below 2^-59 (exact for |v| >= 2^-36).  |v| < 2 is the caller's to ensure
+// (larger values saturate the shift and come out wrong, not out of range).
+DF_HD int64_t float_to_fixed(float v) {
+  const uint32_t b = df::f2u(v);
+  const int e = (int)((b >> 23) & 0xFF);
+  const int64_t m = (int64_t)((b & 0x7FFFFFu) | 0x800000u);
+  const int sh = e > 127 ? 36 : e - 91;  // v 2^59 = m 2^(e - 150 + 59)
+  const int64_t F = sh >= 0 ? (m << sh) : (sh > -63 ? (m >> -sh) : 0);
+  return (b >> 31) ? -F : F;
+}
+
+// A normalised double-float in fixed point: the sum of its halves' images.
+DF_HD int64_t df_to_fixed(df64 c) { return float_to_fixed(c.hi) + float_to_fixed(c.lo); }
+
+// a k / 2^64 rounded to nearest, for the constant corrections below
+// (|a| < 2^63, |k| < 2^31; a's low 32 bits do not take part).
+DF_HD int64_t scale_2m64(int64_t a, int32_t k) {
+  return ((int64_t)(int32_t)(a >> 32) * (int64_t)k + (int64_t(1) << 31)) >> 32;
+}
+
 struct Params {
-  double omb;     // 1 - omega
-  double omw[3];  // omega * w for w0, ws, wd
-  df64 omw_df[3];  // the same as double-float
+  double omb;      // 1 - omega
+  double omw[3];   // omega * w for w0, ws, wd (rounded to binary64)
+  int32_t mass_k;  // rest-population correction, mass_correction()
+  int32_t mom_k;   // correction of J in the 3 c.J terms, momentum_correction()
 };
+
+// The nine constants RN(omega w_q) sum to omega (W0 + 4 WS + 4 WD) less
+// delta, the sum of their exact rounding errors fma(omega, w, -RN(omega w)).
+// Uncorrected, the mass of a cell drifts by delta R per step (about 1e-16,
+// 1e-12 over 10,000 steps) where the reference's drifts by its own rounding.
+// The rest population restores it: its linear term gains (delta / omw0) R,
+// formed as scale_2m64(R, mass_k) with mass_k = delta / omw0 2^64.
+inline int32_t mass_correction(double omega, const double (&w)[3], const double (&omw)[3]) {
+  const double d = fma(omega, w[0], -omw[0]) +
+                   4.0 * (fma(omega, w[1], -omw[1]) + fma(omega, w[2], -omw[2]));
+  const double k = ldexp(d / omw[0], 64);
+  return fabs(k) < 0x1p30 ? (int32_t)llrint(k) : 0;
+}
+
+// The same for the first moment: sum_q c_qx RN(omega w_q) 3 c_qx is
+// 3 (2 omws + 4 omwd), short of 3 omega (2 WS + 4 WD) by 3 (2 e_s + 4 e_d);
+// J in the 3 c.J terms is scaled by 1 + mom_k 2^-64.
+inline int32_t momentum_correction(double omega, const double (&w)[3], const double (&omw)[3]) {
+  const double d = 2.0 * fma(omega, w[1], -omw[1]) + 4.0 * fma(omega, w[2], -omw[2]);
+  const double k = ldexp(d / (2.0 * omw[1] + 4.0 * omw[2]), 64);
+  return fabs(k) < 0x1p30 ? (int32_t)llrint(k) : 0;
+}
 
 // Small terms to binary64: the TRT and RR forms add them with df_to_double
 // (bit-assembled halves and one binary64 add); BGK, whose binary64 pipe is
-// already as busy as its issue, keeps pack_double (integer only).
+// already as busy as its issue, adds them to the fixed-point linear term
+// (integer only) and rounds once.
 
 // BGK in the hybrid arithmetic (in place).  On `bad` the populations are
 // left in an unspecified state: the caller evaluates the cell another way.
@@ -284,27 +336,28 @@ DF_HD void bgk_fast(double (&f)[9], const Params& p, bool& bad) {
   const int64_t d57 = F[5] - F[7], d86 = F[8] - F[6];
   const int64_t JX = (d57 + d86) + (F[1] - F[3]);
   const int64_t JY = (d57 - d86) + (F[2] - F[4]);
-  const double Rd = lin_to_double<SHIFTED>(R);
-  const df64 rho = df::from_double(SHIFTED ? fixed_to_double_fast(R + kOne) : Rd);
+  const df64 rho = df::from_double(fixed_to_double_fast(SHIFTED ? R + kOne : R));
   const df64 inv = df::recip(rho);
   const df64 ux = df::mul(fixed_to_df(JX), inv), uy = df::mul(fixed_to_df(JY), inv);
   const df64 u2_15 = df::mul_f(df::add(df::sqr(ux), df::sqr(uy)), 1.5f);
+  // |C_q| <= rho 9 |u|^2 = 6 rho u2_15 must stay below 2 (NaN fails too)
+  bad |= !(fabsf(rho.hi) * u2_15.hi < 0.3f);
   {
-    const double c0 = df::pack_double(df::neg(df::mul(p.omw_df[0], df::mul(rho, u2_15))));
-    f[0] = fma_d(p.omw[0], Rd, fma_d(p.omb, f[0], c0));
+    const int64_t c0 = df_to_fixed(df::neg(df::mul(rho, u2_15))) + scale_2m64(R, p.mass_k);
+    f[0] = fma_d(p.omw[0], lin_to_double<SHIFTED>(R + c0), p.omb * f[0]);
   }
+  const int64_t JXc = JX + scale_2m64(JX, p.mom_k), JYc = JY + scale_2m64(JY, p.mom_k);
 #define PLBM_HY_PAIR(QP, QM, CU, CJ, WI)                                                    \
   {                                                                                         \
-    const double c = df::pack_double(                                                       \
-        df::mul(p.omw_df[WI], df::mul(rho, df::sub(df::mul_f(df::sqr(CU), 4.5f), u2_15))));  \
+    const int64_t c = df_to_fixed(df::mul(rho, df::sub(df::mul_f(df::sqr(CU), 4.5f), u2_15))); \
     const int64_t cj3 = 3 * (CJ);                                                           \
-    f[QP] = fma_d(p.omw[WI], lin_to_double<SHIFTED>(R + cj3), fma_d(p.omb, f[QP], c));      \
-    f[QM] = fma_d(p.omw[WI], lin_to_double<SHIFTED>(R - cj3), fma_d(p.omb, f[QM], c));      \
+    f[QP] = fma_d(p.omw[WI], lin_to_double<SHIFTED>(R + cj3 + c), p.omb * f[QP]);           \
+    f[QM] = fma_d(p.omw[WI], lin_to_double<SHIFTED>(R - cj3 + c), p.omb * f[QM]);           \
   }
-  PLBM_HY_PAIR(1, 3, ux, JX, 1)
-  PLBM_HY_PAIR(2, 4, uy, JY, 1)
-  PLBM_HY_PAIR(5, 7, df::add(ux, uy), JX + JY, 2)
-  PLBM_HY_PAIR(8, 6, df::sub(ux, uy), JX - JY, 2)
+  PLBM_HY_PAIR(1, 3, ux, JXc, 1)
+  PLBM_HY_PAIR(2, 4, uy, JYc, 1)
+  PLBM_HY_PAIR(5, 7, df::add(ux, uy), JXc + JYc, 2)
+  PLBM_HY_PAIR(8, 6, df::sub(ux, uy), JXc - JYc, 2)
 #undef PLBM_HY_PAIR
 }
 

@@ -266,10 +266,9 @@ hy::Params hybrid_params(double omega) {
   hy::Params p;
   p.omb = 1.0 - omega;
   const double w[3] = {W0, WS, WD};
-  for (int i = 0; i < 3; i++) {
-    p.omw[i] = omega * w[i];
-    p.omw_df[i] = split_const(p.omw[i]);
-  }
+  for (int i = 0; i < 3; i++) p.omw[i] = omega * w[i];
+  p.mass_k = hy::mass_correction(omega, w, p.omw);
+  p.mom_k = hy::momentum_correction(omega, w, p.omw);
   return p;
 }
 
