@@ -28,11 +28,11 @@ struct plbm_batch {
   int ngrids = 0, storage = 0, device = 0, sms = 0, math = PLBM_MATH_FMA;
   std::vector<BatchGrid> grids;   // host copy (off, sizes, params, ty)
   BatchGrid* d_grids = nullptr;
-  int* d_tile_start = nullptr;
+  int2* d_tile_xy = nullptr;    // first cell of each tile (capacity tile_cap)
   int* d_tile_grid = nullptr;   // grid index of each tile (capacity tile_cap)
   size_t tile_cap = 0;
   int small_index = 1;          // every lattice pair has < 2^32 elements
-  int ntiles = 0;
+  int ntiles = 0, nt_bgk = 0;
   long long cells = 0;
   size_t elems = 0, elem_bytes = 8;
   void* base = nullptr;
@@ -78,30 +78,46 @@ void drop_graphs(plbm_batch_t* b) {
   }
 }
 
+// Tiles are numbered grid by grid, the BGK grids' first and the TRT grids'
+// after them, so that the per-step launch can run each kind with its own
+// kernel over a contiguous range; each tile records its grid and first cell.
 int apply_schedule(plbm_batch_t* b) {
-  std::vector<int> start(b->ngrids + 1, 0);
-  for (int i = 0; i < b->ngrids; i++) {
-    BatchGrid& g = b->grids[i];
-    g.ty = b->sched.ty[bucket_of(g.ny)];
-    const int tx = b->sched.threads / g.ty;
-    const long long t = (long long)((g.ny + g.ty - 1) / g.ty) * ((g.nx + tx - 1) / tx);
-    if ((long long)start[i] + t > 0x7fffffffLL) return fail(PLBM_E_INVALID, "too many tiles");
-    start[i + 1] = start[i] + (int)t;
+  std::vector<int> owner;
+  std::vector<int2> xy;
+  b->nt_bgk = 0;
+  for (int pass = 0; pass < 2; pass++) {
+    for (int i = 0; i < b->ngrids; i++) {
+      BatchGrid& g = b->grids[i];
+      if ((g.kind == PLBM_BGK) != (pass == 0)) continue;
+      g.ty = b->sched.ty[bucket_of(g.ny)];
+      g.lty = 0;
+      while ((1 << g.lty) < g.ty) g.lty++;
+      const int tx = b->sched.threads / g.ty;
+      const int tiles_y = (g.ny + g.ty - 1) / g.ty, tiles_x = (g.nx + tx - 1) / tx;
+      if ((long long)owner.size() + (long long)tiles_x * tiles_y > 0x7fffffffLL)
+        return fail(PLBM_E_INVALID, "too many tiles");
+      for (int a = 0; a < tiles_x; a++)
+        for (int c = 0; c < tiles_y; c++) {
+          owner.push_back(i);
+          xy.push_back(make_int2(a * tx, c * g.ty));
+        }
+    }
+    if (pass == 0) b->nt_bgk = (int)owner.size();
   }
-  b->ntiles = start[b->ngrids];
-  std::vector<int> owner((size_t)b->ntiles);
-  for (int i = 0; i < b->ngrids; i++)
-    for (int t = start[i]; t < start[i + 1]; t++) owner[(size_t)t] = i;
+  b->ntiles = (int)owner.size();
   if ((size_t)b->ntiles > b->tile_cap) {
-    if (b->d_tile_grid) cudaFree(b->d_tile_grid);
+    cudaFree(b->d_tile_grid);
+    cudaFree(b->d_tile_xy);
     b->d_tile_grid = nullptr;
+    b->d_tile_xy = nullptr;
     b->tile_cap = 0;
     CUDA_TRY(cudaMalloc(&b->d_tile_grid, sizeof(int) * (size_t)b->ntiles), "cudaMalloc(tile table)");
+    CUDA_TRY(cudaMalloc(&b->d_tile_xy, sizeof(int2) * (size_t)b->ntiles), "cudaMalloc(tile table)");
     b->tile_cap = (size_t)b->ntiles;
   }
   CUDA_TRY(cudaMemcpy(b->d_grids, b->grids.data(), sizeof(BatchGrid) * b->ngrids, cudaMemcpyHostToDevice),
            "upload batch table");
-  CUDA_TRY(cudaMemcpy(b->d_tile_start, start.data(), sizeof(int) * (b->ngrids + 1), cudaMemcpyHostToDevice),
+  CUDA_TRY(cudaMemcpy(b->d_tile_xy, xy.data(), sizeof(int2) * xy.size(), cudaMemcpyHostToDevice),
            "upload tile table");
   CUDA_TRY(cudaMemcpy(b->d_tile_grid, owner.data(), sizeof(int) * owner.size(), cudaMemcpyHostToDevice),
            "upload tile owners");
@@ -117,8 +133,10 @@ int apply_schedule(plbm_batch_t* b) {
 BatchLaunch launch_of(const plbm_batch_t* b) {
   BatchLaunch L;
   L.grids = b->d_grids;
-  L.tile_start = b->d_tile_start;
+  L.tile_xy = b->d_tile_xy;
   L.tile_grid = b->d_tile_grid;
+  L.nt_bgk = b->nt_bgk;
+  L.hybrid = b->math == PLBM_MATH_HYBRID;
   L.small_index = b->small_index;
   L.ngrids = b->ngrids;
   L.ntiles = b->ntiles;
@@ -216,7 +234,6 @@ extern "C" int plbm_batch_create(int ngrids, const int* nx, const int* ny, const
   cudaError_t e = cudaMalloc(&b->base, off * b->elem_bytes);
   if (e == cudaSuccess) e = cudaMemset(b->base, 0, off * b->elem_bytes);
   if (e == cudaSuccess) e = cudaMalloc(&b->d_grids, sizeof(BatchGrid) * ngrids);
-  if (e == cudaSuccess) e = cudaMalloc(&b->d_tile_start, sizeof(int) * (ngrids + 1));
   if (e == cudaSuccess) e = cudaMalloc(&b->ctrl, batch_ctrl_bytes());
   if (e == cudaSuccess) e = cudaMemset(b->ctrl, 0, batch_ctrl_bytes());
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->own, cudaStreamNonBlocking);
@@ -241,7 +258,7 @@ extern "C" int plbm_batch_destroy(plbm_batch_t* b) {
   drop_graphs(b);
   cudaFree(b->base);
   cudaFree(b->d_grids);
-  cudaFree(b->d_tile_start);
+  cudaFree(b->d_tile_xy);
   cudaFree(b->d_tile_grid);
   cudaFree(b->ctrl);
   cudaFree(b->scratch);

@@ -5,15 +5,18 @@
 // with two lattices A and B, all grids packed into one device allocation.
 // Work unit: a tile of TY x TX cells of one grid (TY rows along the fast y
 // axis, TX = threads / TY columns), TY chosen per grid by the schedule.  The
-// tiles of all grids are numbered 0..T-1; CTA b takes tiles b, b + nCTA, ...
+// tiles of all grids are numbered 0..T-1, the BGK grids' first; a table holds
+// each tile's grid and first cell.  Persistent CTA b takes tiles b, b + nCTA,
+// ...; the per-step launch gives each tile its own CTA.
 //
 // Two launch modes, both capturable in a CUDA graph:
 //   * persistent: ONE cooperative launch runs all steps; the CTAs meet at a
 //     grid-wide barrier between steps.  Every wait on the barrier is bounded:
 //     after kSpinLimit polls the CTA records a timeout in the control block and
 //     the kernel returns, so a lost CTA cannot hang the GPU.
-//   * per-step: one ordinary launch per step (the graph then holds one node
-//     per step).
+//   * per-step: ordinary launches, one per collision kind and step (the graph
+//     then holds those nodes); with 128-thread CTAs each kind runs a kernel
+//     compiled for it alone.
 //
 // Lattice loads use ld.global.cg (L2 only): in the persistent kernel a lattice
 // written in step s by other SMs is read in step s+1, and the non-coherent L1 /
@@ -66,20 +69,20 @@ __device__ __noinline__ void fallback_cell(const double* __restrict__ src, doubl
 
 // Process one tile of one grid for one step.  I: index type inside one grid's
 // lattice pair (32-bit when every grid's pair has fewer than 2^32 elements).
-// gp is the grid's table entry; its relaxation constants are read where they
-// are used (through the read-only path) rather than held in registers.
-template <class S, bool CG, typename I>
-__device__ __forceinline__ void do_tile(const BatchGrid* __restrict__ gp, int local_tile, int parity,
+// KIND: K_BGK or K_TRT, or -1 for the grid's own (read at run time); HY: 1
+// hybrid binary64, 0 the binary64 operator, -1 the grid's flag.  gp is the
+// grid's table entry; its relaxation constants are read where they are used
+// (through the read-only path) rather than held in registers.  (x0, y0) is
+// the tile's first cell; its TY = 2^lty rows run along y.
+template <class S, bool CG, typename I, int KIND = -1, int HY = -1>
+__device__ __forceinline__ void do_tile(const BatchGrid* __restrict__ gp, int2 xy, int parity,
                                         typename S::elem* __restrict__ base) {
   const int nx = __ldg(&gp->nx), ny = __ldg(&gp->ny), ld = __ldg(&gp->ld);
-  const int ty = __ldg(&gp->ty);
-  const int tx = blockDim.x / ty;
-  const int tiles_y = (ny + ty - 1) / ty;
-  const int txi = local_tile / tiles_y, tyi = local_tile - txi * tiles_y;
-  const int y = tyi * ty + (int)(threadIdx.x % ty);
-  const int x = txi * tx + (int)(threadIdx.x / ty);
+  const int lty = __ldg(&gp->lty);
+  const int y = xy.y + (int)(threadIdx.x & ((1u << lty) - 1u));
+  const int x = xy.x + (int)(threadIdx.x >> lty);
   if (x >= nx || y >= ny) return;
-  const int kind = __ldg(&gp->kind);
+  const int kind = KIND >= 0 ? KIND : __ldg(&gp->kind);
   const long long goff = __ldg(&gp->off);
   const I L = (I)ld, P = (I)ld * (I)nx, lat = 9 * P;
   const typename S::elem* src = base + goff + (parity ? lat : 0);
@@ -104,7 +107,7 @@ __device__ __forceinline__ void do_tile(const BatchGrid* __restrict__ gp, int lo
     if (kind == K_TRT) collide_shift<K_TRT, typename S::real>(f, gp->p);
     else collide_shift<K_BGK, typename S::real>(f, gp->p);
   } else {
-    if (__ldg(&gp->hybrid)) {
+    if (HY > 0 || (HY < 0 && __ldg(&gp->hybrid))) {
       bool bad = false;
       if (kind == K_TRT) hy::trt_fast(f, gp->ht, bad);
       else hy::bgk_fast(f, gp->hp, bad);
@@ -124,15 +127,13 @@ __device__ __forceinline__ void do_tile(const BatchGrid* __restrict__ gp, int lo
 }
 
 // Tiles t = blockIdx.x, blockIdx.x + gridDim.x, ...; the grid of tile t is
-// tile_grid[t] (precomputed), its first tile tile_start[grid].
+// tile_grid[t], its first cell tile_xy[t] (both precomputed).
 template <class S, bool CG, typename I>
-__device__ __forceinline__ void sweep(const BatchGrid* __restrict__ grids, const int* __restrict__ tile_start,
+__device__ __forceinline__ void sweep(const BatchGrid* __restrict__ grids, const int2* __restrict__ tile_xy,
                                       const int* __restrict__ tile_grid, int ntiles, int parity,
                                       typename S::elem* base) {
-  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    const int gi = __ldg(tile_grid + t);
-    do_tile<S, CG, I>(grids + gi, t - __ldg(tile_start + gi), parity, base);
-  }
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x)
+    do_tile<S, CG, I>(grids + __ldg(tile_grid + t), __ldg(tile_xy + t), parity, base);
 }
 
 // Grid-wide barrier with a bounded wait.  Returns false when the wait ran out
@@ -170,34 +171,51 @@ __device__ __forceinline__ bool barrier(Ctrl* ctrl, int step) {
 
 template <class S, typename I>
 __global__ void __launch_bounds__(kBatchMaxThreads) k_batch_persistent(const BatchGrid* __restrict__ grids,
-                                                                      const int* __restrict__ tile_start,
+                                                                      const int2* __restrict__ tile_xy,
                                                                       const int* __restrict__ tile_grid,
                                                                       int ntiles, int nsteps, int parity0,
                                                                       typename S::elem* base, Ctrl* ctrl) {
   for (int s = 0; s < nsteps; s++) {
-    sweep<S, true, I>(grids, tile_start, tile_grid, ntiles, (parity0 + s) & 1, base);
+    sweep<S, true, I>(grids, tile_xy, tile_grid, ntiles, (parity0 + s) & 1, base);
     if (s + 1 < nsteps && !barrier(ctrl, s)) return;
   }
 }
 
 template <class S, typename I>
 __global__ void __launch_bounds__(kBatchMaxThreads) k_batch_step(const BatchGrid* __restrict__ grids,
-                                                                const int* __restrict__ tile_start,
+                                                                const int2* __restrict__ tile_xy,
                                                                 const int* __restrict__ tile_grid, int ntiles,
                                                                 int parity, typename S::elem* base) {
-  sweep<S, false, I>(grids, tile_start, tile_grid, ntiles, parity, base);
+  sweep<S, false, I>(grids, tile_xy, tile_grid, ntiles, parity, base);
 }
 
-// The same for 128-thread CTAs with at least 6 resident per SM (at most 80
-// registers).  The binary64 hybrid tiles otherwise take 97 registers and 20
-// resident warps per SM; with the cap (a few bytes of spills) the 512-grid
-// batch runs 22 % faster.
-template <class S, typename I>
-__global__ void __launch_bounds__(128, 6) k_batch_step_128(const BatchGrid* __restrict__ grids,
-                                                          const int* __restrict__ tile_start,
-                                                          const int* __restrict__ tile_grid, int ntiles, int parity,
-                                                          typename S::elem* base) {
-  sweep<S, false, I>(grids, tile_start, tile_grid, ntiles, parity, base);
+// Per-step launch of 128-thread CTAs over the tiles of one collision kind
+// (tile t0 + blockIdx.x), compiled for that kind and arithmetic alone with
+// MINB resident CTAs per SM: the binary64 hybrid BGK tiles fit 56 registers
+// (9 CTAs) and the TRT tiles 72 (7).  One kernel for both kinds needed 97
+// registers, 80 under a cap with spills; the 512-grid binary64 hybrid batch
+// runs 24.5k MLUPS split this way against 20.9k (24.1k with caps 10 / 8).
+template <class S, typename I, int KIND, int HY, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_batch_kind(const BatchGrid* __restrict__ grids,
+                                                         const int2* __restrict__ tile_xy,
+                                                         const int* __restrict__ tile_grid, int t0, int parity,
+                                                         typename S::elem* base) {
+  const int t = t0 + (int)blockIdx.x;
+  do_tile<S, false, I, KIND, HY>(grids + __ldg(tile_grid + t), __ldg(tile_xy + t), parity, base);
+}
+
+template <class S, typename I, int HY>
+cudaError_t launch_kinds(const BatchLaunch& L, int parity) {
+  typedef typename S::elem E;
+  E* base = static_cast<E*>(L.base);
+  const int ntrt = L.ntiles - L.nt_bgk;
+  if (L.nt_bgk > 0)
+    k_batch_kind<S, I, K_BGK, HY, (HY > 0 ? 9 : 8)><<<L.nt_bgk, 128, 0, L.stream>>>(L.grids, L.tile_xy, L.tile_grid,
+                                                                                    0, parity, base);
+  if (ntrt > 0)
+    k_batch_kind<S, I, K_TRT, HY, 7><<<ntrt, 128, 0, L.stream>>>(L.grids, L.tile_xy, L.tile_grid, L.nt_bgk, parity,
+                                                                 base);
+  return cudaGetLastError();
 }
 
 template <class S, typename I>
@@ -215,19 +233,20 @@ cudaError_t launch_batch(const BatchLaunch& L, int nsteps, int parity0) {
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, k_batch_persistent<S, I>, L.grids, L.tile_start, L.tile_grid, L.ntiles, nsteps,
+    return cudaLaunchKernelEx(&cfg, k_batch_persistent<S, I>, L.grids, L.tile_xy, L.tile_grid, L.ntiles, nsteps,
                               parity0, base, ctrl);
   }
-  // one tile per CTA
-  const bool capped = L.threads == 128;
+  // one tile per CTA; 128-thread CTAs run one kernel per collision kind
   for (int s = 0; s < nsteps; s++) {
-    if (capped)
-      k_batch_step_128<S, I><<<L.ntiles, L.threads, 0, L.stream>>>(L.grids, L.tile_start, L.tile_grid, L.ntiles,
-                                                                   (parity0 + s) & 1, base);
-    else
-      k_batch_step<S, I><<<L.ntiles, L.threads, 0, L.stream>>>(L.grids, L.tile_start, L.tile_grid, L.ntiles,
-                                                               (parity0 + s) & 1, base);
-    cudaError_t e = cudaGetLastError();
+    const int parity = (parity0 + s) & 1;
+    cudaError_t e;
+    if (L.threads == 128) {
+      e = (!S::ddf && L.hybrid) ? launch_kinds<S, I, 1>(L, parity) : launch_kinds<S, I, 0>(L, parity);
+    } else {
+      k_batch_step<S, I><<<L.ntiles, L.threads, 0, L.stream>>>(L.grids, L.tile_xy, L.tile_grid, L.ntiles, parity,
+                                                               base);
+      e = cudaGetLastError();
+    }
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;

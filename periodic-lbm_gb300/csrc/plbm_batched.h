@@ -19,7 +19,8 @@ struct alignas(16) BatchGrid {
   int kind;           // K_BGK or K_TRT
   int ty;             // tile rows along y; tile columns = threads / ty
   int hybrid;         // binary64 grid in hybrid arithmetic
-  int pad[2];
+  int lty;            // log2(ty)
+  int pad;
 };
 
 hy::Params hybrid_params(double omega);
@@ -27,9 +28,11 @@ hy::TrtParams hybrid_trt_params(const CollParams& p);
 
 struct BatchLaunch {
   const BatchGrid* grids;  // device
-  const int* tile_start;   // device, ngrids + 1 prefix sums of tiles
+  const int2* tile_xy;     // device, first cell (x0, y0) of each tile
   const int* tile_grid;    // device, grid index of each tile
   int ngrids, ntiles;
+  int nt_bgk;              // tiles [0, nt_bgk) belong to BGK grids, the rest to TRT grids
+  int hybrid;              // binary64 grids in hybrid arithmetic (batch-wide)
   int threads, ctas;       // ctas: persistent mode only (per-step: one CTA per tile)
   int persistent;          // 1: one cooperative launch for all steps
   int small_index;         // every grid's lattice pair has < 2^32 elements
