@@ -161,3 +161,64 @@ def test_lattice_past_2_32_elements(gpu_lib, math_mode):
                 assert np.array_equal(sub, b[inner, inner]), (x0, y0)
             else:
                 assert np.max(np.abs(sub - b[inner, inner])) <= 1e-12 * sc, (x0, y0)
+
+
+@pytest.mark.parametrize("math_mode,threads,persistent", [("hybrid", 128, 0), ("fma", 128, 0), ("hybrid", 256, 1)])
+def test_batched_512_grids_against_oracle(gpu_lib, math_mode, threads, persistent):
+    """The bench's batched workload at its full size: 512 Taylor-Green grids of
+    uneven sizes (32..1024 per side, 39.1 M cells) and relaxation times, BGK and
+    TRT, 5 steps; every grid's rho, u against the oracle within 1e-12.  The
+    per-step 128-thread launch (one kernel per collision kind) and the
+    persistent kernel."""
+    from plbm import batched
+    from plbm.batched import Schedule
+    specs, flds = batched.random_tgv_batch(512, 2024)
+    b = batched.BatchedGrids(specs, "f64", math=math_mode)
+    fields = [batched.tgv_fields(*fl) for fl in flds]
+    for i, f in enumerate(fields):
+        b.set_equilibrium(i, *f)
+    b.schedule = Schedule.from_dict({"threads": threads, "ctas_per_sm": 0, "persistent": persistent,
+                                     "ty": [32, 32, 64, 64, 64]})
+    steps = 5
+    b.run(steps)
+    b.synchronize()
+    kinds = {"bgk": KIND["bgk"], "trt": KIND["trt"]}
+    for i, sp in enumerate(specs):
+        f2 = np.empty((2, 9, sp.nx, O.pad16(sp.ny)))
+        f2[1] = O.set_pdf_to_equilibrium(*fields[i])
+        iold, _ = O.perform_lbm_step(f2, sp.ny, 2, 1, kinds[sp.kind], sp.omega, sp.trt_magic, steps)
+        got = b.download(i)
+        for a, c in zip(O.update_macros(got, sp.ny), O.update_macros(f2[iold - 1], sp.ny)):
+            assert relinf(a, c) <= 1e-12, (i, sp)
+    b.close()
+
+
+@pytest.mark.parametrize("math_mode", ["strict", "hybrid"])
+def test_plugin_bench_size_against_oracle(gpu_lib, math_mode):
+    """The sim/ plugin ABI (shifted binary64 BGK, collide then push) on an
+    8192^2 Taylor-Green state, 3 steps, against the oracle's restatement of
+    sim/sim_slbm.F90: strict bit-identical, hybrid within 1e-12."""
+    need_memory(48, 24)
+    from plbm.plugin import SimPlugin, make_params
+    n, omega, steps = 8192, 1.0 / 0.6, 3
+    k = 2 * math.pi / n
+    x = (np.arange(n) + 0.5) * k
+    u = np.empty((n, n, 2), order="F")
+    u[:, :, 0] = -0.05 * np.outer(np.cos(x), np.sin(x))
+    u[:, :, 1] = 0.05 * np.outer(np.sin(x), np.cos(x))
+    p = np.asfortranarray(-0.25 * 0.05 ** 2 * (np.cos(2 * x)[:, None] + np.cos(2 * x)[None, :]))
+    sim = SimPlugin()
+    sim.init((n, n), 1.0, p, u, params=make_params(math=math_mode))
+    sim.steps(omega, steps)
+    rho, uu = sim.vars()
+    sim.free()
+    f = O.sim_eqinit(p.T, u[:, :, 0].T, u[:, :, 1].T)
+    f = O.sim_slbm_steps(f, omega, steps)
+    r, ux, uy = (a.T for a in O.sim_macros(f))
+    del f
+    if math_mode == "strict":
+        assert np.array_equal(rho, r)
+        assert np.array_equal(uu[:, :, 0], ux) and np.array_equal(uu[:, :, 1], uy)
+    else:
+        assert relinf(rho, r) <= 1e-12
+        assert relinf(uu[:, :, 0], ux) <= 1e-12 and relinf(uu[:, :, 1], uy) <= 1e-12

@@ -170,6 +170,26 @@ def test_plugin_hybrid_bgk_within_1e12(gpu_lib):
     assert rel(uu[:, :, 0], ux) <= 1e-12 and rel(uu[:, :, 1], uy) <= 1e-12
 
 
+@pytest.mark.parametrize("tau", [0.6, 0.55])
+def test_plugin_hybrid_bgk_long_horizon(gpu_lib, tau):
+    """10,000 plugin steps (sim/ BGK, shifted binary64, hybrid arithmetic) of a
+    256 x 192 TGV (amplitude decays by ~e^-1.1) against the oracle: the rounded
+    constants' mass and momentum factors are corrected on DH = sum h and J as in
+    the unshifted form."""
+    from plbm.plugin import SimPlugin, make_params
+    nx, ny, steps = 256, 192, 10000
+    p, u = tgv_fields(nx, ny, umax=0.05)
+    sim = SimPlugin()
+    sim.init((nx, ny), 1.0, p, u, params=make_params(math="hybrid"))
+    sim.steps(1.0 / tau, steps)
+    rho, uu = sim.vars()
+    sim.free()
+    r, ux, uy = oracle_run(p, u, 1.0 / tau, steps)
+    rel = lambda a, b: np.max(np.abs(a - b)) / np.max(np.abs(b))  # noqa: E731
+    assert rel(rho, r) <= 1e-12
+    assert rel(uu[:, :, 0], ux) <= 1e-12 and rel(uu[:, :, 1], uy) <= 1e-12
+
+
 @pytest.mark.parametrize("kind", ["trt", "rr"])
 def test_plugin_hybrid_other_collisions_match_fma(gpu_lib, kind):
     from plbm.plugin import SimPlugin, make_params
