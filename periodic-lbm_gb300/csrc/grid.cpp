@@ -23,6 +23,20 @@
 
 using namespace plbm;
 
+int plbm::block_for(long long cells) {
+  static int sms[64] = {0};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return kBlock;
+  if (!sms[dev]) {
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1) return kBlock;
+    sms[dev] = n;
+  }
+  const long long per_sm = (cells + sms[dev] - 1) / sms[dev];
+  if (per_sm >= kBlock) return kBlock;
+  return (int)(per_sm < 32 ? 32 : (per_sm + 31) / 32 * 32);
+}
+
 // ---------------------------------------------------------------------------
 // error reporting
 namespace plbm_internal {
@@ -121,6 +135,7 @@ extern "C" int plbm_grid_destroy(plbm_grid_t* g) {
   if (g->f) cudaFree(g->f);
   if (g->spare) cudaFree(g->spare);
   if (g->scratch) cudaFree(g->scratch);
+  if (g->step_graph) cudaGraphExecDestroy(g->step_graph);
   if (g->own) cudaStreamDestroy(g->own);
   delete g;
   return PLBM_OK;
@@ -402,6 +417,73 @@ extern "C" int plbm_collide(plbm_grid_t* g) {
   return ok();
 }
 
+namespace {
+
+// Small grids: one step is a few microseconds of GPU work, less than the
+// host's cost of a launch, so a loop of launches leaves the GPU idle.  The
+// loop is captured once as a CUDA graph of kGraphSteps (even) fused steps,
+// lattice iold -> inew -> iold ..., and replayed; an even count leaves iold
+// and inew where they were.
+constexpr int kGraphSteps = 16;
+constexpr long long kGraphCells = 1ll << 17;
+
+bool graph_key_matches(const plbm_grid_t* g, const void* a, const void* b) {
+  const auto& k = g->step_key;
+  return g->step_graph && k.a == a && k.b == b && k.stream == g->stream && k.kind == g->kind &&
+         k.math == g->math && k.streaming == g->streaming && k.omega == g->omega &&
+         k.trt_magic == g->trt_magic && k.dt == g->dt;
+}
+
+// Replays the captured loop `reps` times (capturing it first when needed).
+// Returns cudaErrorNotSupported when the stream cannot be captured (the
+// caller's own capture is in progress): the caller then launches step by step.
+cudaError_t replay_step_graph(plbm_grid_t* g, const CollParams& p, int reps) {
+  void* a = lattice(g, g->iold);
+  void* b = lattice(g, g->inew);
+  if (!graph_key_matches(g, a, b)) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaError_t e = cudaStreamIsCapturing(g->stream, &cs);
+    if (e != cudaSuccess) return e;
+    if (cs != cudaStreamCaptureStatusNone) return cudaErrorNotSupported;
+    if (g->step_graph) cudaGraphExecDestroy(g->step_graph);
+    g->step_graph = nullptr;
+    e = cudaStreamBeginCapture(g->stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return e;
+    cudaError_t le = cudaSuccess;
+    for (int i = 0; i < kGraphSteps && le == cudaSuccess; i++)
+      le = fused_step(g, i % 2 ? b : a, i % 2 ? a : b, p);
+    cudaGraph_t graph = nullptr;
+    e = cudaStreamEndCapture(g->stream, &graph);
+    if (le != cudaSuccess || e != cudaSuccess) {
+      if (graph) cudaGraphDestroy(graph);
+      return le != cudaSuccess ? le : e;
+    }
+    e = cudaGraphInstantiate(&g->step_graph, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+      g->step_graph = nullptr;
+      return e;
+    }
+    auto& k = g->step_key;
+    k.a = a;
+    k.b = b;
+    k.stream = g->stream;
+    k.kind = g->kind;
+    k.math = g->math;
+    k.streaming = g->streaming;
+    k.omega = g->omega;
+    k.trt_magic = g->trt_magic;
+    k.dt = g->dt;
+  }
+  for (int r = 0; r < reps; r++) {
+    cudaError_t e = cudaGraphLaunch(g->step_graph, g->stream);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+}  // namespace
+
 extern "C" int plbm_perform_lbm_step(plbm_grid_t* g, int nsteps) {
   if (int r = check_grid(g)) return r;
   if (nsteps < 0) return fail(PLBM_E_INVALID, "nsteps = %d < 0", nsteps);
@@ -412,6 +494,15 @@ extern "C" int plbm_perform_lbm_step(plbm_grid_t* g, int nsteps) {
   if (int r = check_scheme(g)) return r;
   if (int r = use_device(g)) return r;
   const CollParams p = plbm_make_params(g->omega, g->trt_magic);
+  if ((long long)g->nx * g->ny <= kGraphCells && nsteps >= 2 * kGraphSteps) {
+    const int reps = nsteps / kGraphSteps;
+    cudaError_t e = replay_step_graph(g, p, reps);
+    if (e == cudaSuccess) {
+      nsteps -= reps * kGraphSteps;  // even: iold, inew unchanged
+    } else if (e != cudaErrorNotSupported) {
+      return cuda_fail(e, "stream-collide graph");
+    }
+  }
   for (int i = 0; i < nsteps; i++) {
     cudaError_t e = fused_step(g, lattice(g, g->iold), lattice(g, g->inew), p);
     if (e != cudaSuccess) return cuda_fail(e, "stream-collide kernel");

@@ -40,6 +40,16 @@ struct plbm_grid {
   cudaStream_t stream = nullptr;
   double* scratch = nullptr;   // 3*nx*ny doubles + reduction partials
   size_t scratch_elems = 0;
+  // Captured step loop of a small grid (plbm_perform_lbm_step) and what it
+  // was captured for; recaptured when any of it changes.
+  cudaGraphExec_t step_graph = nullptr;
+  struct {
+    const void* a = nullptr;
+    const void* b = nullptr;
+    cudaStream_t stream = nullptr;
+    int kind = -1, math = -1, streaming = -1;
+    double omega = 0, trt_magic = 0, dt = 0;
+  } step_key;
 };
 
 namespace plbm_internal {

@@ -18,6 +18,14 @@ struct Sweep {
 // Threads per block of the per-cell kernels.
 constexpr int kBlock = 256;
 
+// Threads per block for a fused step over `cells` cells: kBlock, or, for a
+// grid with fewer than kBlock cells per SM, the smallest multiple of 32 that
+// covers the grid with one CTA per SM.  A small grid then spreads over every
+// SM instead of a few: each SM's binary64 pipe retires about 2 FMAs per
+// cycle, so a 64^2 grid in 16 CTAs of 256 threads spent ~4.5 us per step in
+// its collision arithmetic.
+int block_for(long long cells);
+
 // The binary64 reference kernels exist twice, once compiled with FMA
 // contraction (namespace fma) and once without (namespace strict).
 #define PLBM_DECLARE_F64(NS)                                                              \

@@ -119,16 +119,17 @@ inline int tiles(int n) { return (n + kBlock - 1) / kBlock; }
 
 template <class L, class S, bool PUSH>
 cudaError_t launch_dev(int kind, const Sweep& s, const CollParams& p) {
-  const int ft = tiles(L::x_fast ? s.nx : s.ny);
+  const int bs = block_for((long long)s.nx * s.ny);
+  const int ft = ((L::x_fast ? s.nx : s.ny) + bs - 1) / bs;
   const long long blocks = (long long)ft * (L::x_fast ? s.ny : s.nx);
   if (blocks <= 0 || blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
   typedef typename S::elem E;
   const E* a = static_cast<const E*>(s.src);
   E* b = static_cast<E*>(s.dst);
   switch (kind) {
-    case K_BGK: k_step_dev<L, S, K_BGK, PUSH><<<(unsigned)blocks, kBlock, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft, p); break;
-    case K_TRT: k_step_dev<L, S, K_TRT, PUSH><<<(unsigned)blocks, kBlock, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft, p); break;
-    case K_RR: k_step_dev<L, S, K_RR, PUSH><<<(unsigned)blocks, kBlock, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft, p); break;
+    case K_BGK: k_step_dev<L, S, K_BGK, PUSH><<<(unsigned)blocks, bs, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft, p); break;
+    case K_TRT: k_step_dev<L, S, K_TRT, PUSH><<<(unsigned)blocks, bs, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft, p); break;
+    case K_RR: k_step_dev<L, S, K_RR, PUSH><<<(unsigned)blocks, bs, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft, p); break;
     default: return cudaErrorNotSupported;
   }
   return cudaGetLastError();
@@ -152,7 +153,8 @@ cudaError_t launch_collide_dev(int kind, const Sweep& s, const CollParams& p) {
 
 template <class S, typename I>
 cudaError_t launch_pull_dev(int kind, const Sweep& s, const CollParams& cp) {
-  const int ft = tiles(s.ny);
+  const int bs = block_for((long long)s.nx * s.ny);
+  const int ft = (s.ny + bs - 1) / bs;
   const long long blocks = (long long)ft * s.nx;
   if (blocks <= 0 || blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
   typedef typename S::elem E;
@@ -161,9 +163,9 @@ cudaError_t launch_pull_dev(int kind, const Sweep& s, const CollParams& cp) {
   const ShiftParamsF p = shift_params(kind, cp);
   const unsigned nb = (unsigned)blocks;
   switch (kind) {
-    case K_BGK: k_step_dev_pull<S, K_BGK, I><<<nb, kBlock, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft, p); break;
-    case K_TRT: k_step_dev_pull<S, K_TRT, I><<<nb, kBlock, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft, p); break;
-    case K_RR: k_step_dev_pull<S, K_RR, I><<<nb, kBlock, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft, p); break;
+    case K_BGK: k_step_dev_pull<S, K_BGK, I><<<nb, bs, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft, p); break;
+    case K_TRT: k_step_dev_pull<S, K_TRT, I><<<nb, bs, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft, p); break;
+    case K_RR: k_step_dev_pull<S, K_RR, I><<<nb, bs, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft, p); break;
     default: return cudaErrorNotSupported;
   }
   return cudaGetLastError();

@@ -250,13 +250,13 @@ __global__ void __launch_bounds__(kBlock, hybrid_min_blocks(KIND)) k_push_hybrid
 }
 
 template <int KIND>
-cudaError_t launch_hybrid(const Sweep& s, unsigned blocks, int ft, const HybridArgs& a) {
+cudaError_t launch_hybrid(const Sweep& s, unsigned blocks, int bs, int ft, const HybridArgs& a) {
   const double* src = static_cast<const double*>(s.src);
   double* dst = static_cast<double*>(s.dst);
   if ((unsigned long long)s.ld * (unsigned long long)s.nx * 9ull < (1ull << 32))
-    k_step_hybrid<uint32_t, KIND><<<blocks, kBlock, 0, s.stream>>>(src, dst, s.nx, s.ny, s.ld, ft, a);
+    k_step_hybrid<uint32_t, KIND><<<blocks, bs, 0, s.stream>>>(src, dst, s.nx, s.ny, s.ld, ft, a);
   else
-    k_step_hybrid<size_t, KIND><<<blocks, kBlock, 0, s.stream>>>(src, dst, s.nx, s.ny, s.ld, ft, a);
+    k_step_hybrid<size_t, KIND><<<blocks, bs, 0, s.stream>>>(src, dst, s.nx, s.ny, s.ld, ft, a);
   return cudaGetLastError();
 }
 
@@ -305,7 +305,8 @@ hy::RrParams hybrid_rr_params(const CollParams& cp) {
 
 cudaError_t step_pull_df64(int kind, const Sweep& s, const CollParams& cp) {
   if (kind != K_BGK && kind != K_TRT && kind != K_RR) return cudaErrorNotSupported;
-  const int ft = (s.ny + kBlock - 1) / kBlock;
+  const int bs = block_for((long long)s.nx * s.ny);
+  const int ft = (s.ny + bs - 1) / bs;
   const long long blocks = (long long)ft * s.nx;
   if (blocks <= 0 || blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
   HybridArgs a;
@@ -313,14 +314,15 @@ cudaError_t step_pull_df64(int kind, const Sweep& s, const CollParams& cp) {
   a.trt = hybrid_trt_params(cp);
   a.rr = hybrid_rr_params(cp);
   a.ref = cp;
-  if (kind == K_TRT) return launch_hybrid<K_TRT>(s, (unsigned)blocks, ft, a);
-  if (kind == K_RR) return launch_hybrid<K_RR>(s, (unsigned)blocks, ft, a);
-  return launch_hybrid<K_BGK>(s, (unsigned)blocks, ft, a);
+  if (kind == K_TRT) return launch_hybrid<K_TRT>(s, (unsigned)blocks, bs, ft, a);
+  if (kind == K_RR) return launch_hybrid<K_RR>(s, (unsigned)blocks, bs, ft, a);
+  return launch_hybrid<K_BGK>(s, (unsigned)blocks, bs, ft, a);
 }
 
 cudaError_t step_push_hybrid(int kind, const Sweep& s, const CollParams& cp) {
   if (kind != K_BGK && kind != K_TRT && kind != K_RR) return cudaErrorNotSupported;
-  const int ft = (s.nx + kBlock - 1) / kBlock;
+  const int bs = block_for((long long)s.nx * s.ny);
+  const int ft = (s.nx + bs - 1) / bs;
   const long long blocks = (long long)ft * s.ny;
   if (blocks <= 0 || blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
   HybridArgs a;
@@ -334,9 +336,9 @@ cudaError_t step_push_hybrid(int kind, const Sweep& s, const CollParams& cp) {
   const bool small = (unsigned long long)s.ld * (unsigned long long)s.ny * 9ull < (1ull << 32);
 #define PLBM_PUSH_HY(I)                                                                                      \
   switch (kind) {                                                                                            \
-    case K_BGK: k_push_hybrid<I, K_BGK><<<nb, kBlock, 0, s.stream>>>(src, dst, s.nx, s.ny, s.ld, ft, a); break; \
-    case K_TRT: k_push_hybrid<I, K_TRT><<<nb, kBlock, 0, s.stream>>>(src, dst, s.nx, s.ny, s.ld, ft, a); break; \
-    default: k_push_hybrid<I, K_RR><<<nb, kBlock, 0, s.stream>>>(src, dst, s.nx, s.ny, s.ld, ft, a); break;     \
+    case K_BGK: k_push_hybrid<I, K_BGK><<<nb, bs, 0, s.stream>>>(src, dst, s.nx, s.ny, s.ld, ft, a); break; \
+    case K_TRT: k_push_hybrid<I, K_TRT><<<nb, bs, 0, s.stream>>>(src, dst, s.nx, s.ny, s.ld, ft, a); break; \
+    default: k_push_hybrid<I, K_RR><<<nb, bs, 0, s.stream>>>(src, dst, s.nx, s.ny, s.ld, ft, a); break;     \
   }
   if (small) {
     PLBM_PUSH_HY(uint32_t)

@@ -173,19 +173,21 @@ inline int tiles(int n) { return (n + kBlock - 1) / kBlock; }
 
 template <class L, bool SHIFT, bool PUSH>
 cudaError_t launch_step(int kind, const Sweep& s, const CollParams& p) {
-  const int ft = tiles(L::x_fast ? s.nx : s.ny);
+  const int bs = block_for((long long)s.nx * s.ny);
+  const int nfast = L::x_fast ? s.nx : s.ny;
+  const int ft = (nfast + bs - 1) / bs;
   const int nslow = L::x_fast ? s.ny : s.nx;
   const long long blocks = (long long)ft * nslow;
   if (blocks <= 0 || blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
   const double* a = static_cast<const double*>(s.src);
   double* b = static_cast<double*>(s.dst);
   switch (kind) {
-    case K_BGK: k_step<L, K_BGK, SHIFT, PUSH><<<(unsigned)blocks, kBlock, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft, p); break;
-    case K_TRT: k_step<L, K_TRT, SHIFT, PUSH><<<(unsigned)blocks, kBlock, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft, p); break;
-    case K_RR: k_step<L, K_RR, SHIFT, PUSH><<<(unsigned)blocks, kBlock, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft, p); break;
+    case K_BGK: k_step<L, K_BGK, SHIFT, PUSH><<<(unsigned)blocks, bs, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft, p); break;
+    case K_TRT: k_step<L, K_TRT, SHIFT, PUSH><<<(unsigned)blocks, bs, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft, p); break;
+    case K_RR: k_step<L, K_RR, SHIFT, PUSH><<<(unsigned)blocks, bs, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft, p); break;
     case K_BGKI:
       if (SHIFT) return cudaErrorNotSupported;
-      k_step<L, K_BGKI, false, PUSH><<<(unsigned)blocks, kBlock, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft, p);
+      k_step<L, K_BGKI, false, PUSH><<<(unsigned)blocks, bs, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft, p);
       break;
     default: return cudaErrorInvalidValue;
   }

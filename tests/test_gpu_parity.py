@@ -175,6 +175,37 @@ def test_hybrid_long_horizon_bench_state(gpu_lib, kind, tau):
         assert relinf(a, b) <= TOL
 
 
+@pytest.mark.parametrize("math_mode,kind", [("strict", "bgk"), ("hybrid", "trt"), ("fma", "rr")])
+def test_small_grid_graph_replay_equals_single_steps(gpu_lib, math_mode, kind):
+    """perform_lbm_step(n) on a small grid replays a captured loop of steps; the
+    lattices and buffer indices equal n single-step calls, across odd counts,
+    a change of relaxation (recapture) and a change of stream."""
+    import torch
+    from plbm import LatticeGrid
+    nx, ny = 40, 24
+    f0 = initial_state(nx, ny, u0=0.03)
+    grids = [LatticeGrid(nx, ny, collision=kind, math=math_mode) for _ in range(2)]
+    for g in grids:
+        g.set_relaxation(1.4, 0.25)
+        g.upload(f0, g.iold)
+    plan = [(37, 1.4), (64, 1.4), (33, 1.7), (40, 1.7)]
+    for i, (n, omega) in enumerate(plan):
+        if i == 3:
+            st = torch.cuda.Stream()
+            for g in grids:
+                g.set_stream(st.cuda_stream)
+        for g in grids:
+            g.set_relaxation(omega, 0.25)
+        grids[0].perform_lbm_step(n)
+        for _ in range(n):
+            grids[1].perform_lbm_step(1)
+        assert grids[0].indices == grids[1].indices
+        a, b = (g.download(g.iold) for g in grids)
+        assert np.array_equal(a[:, :, :ny], b[:, :, :ny])
+    for g in grids:
+        g.close()
+
+
 def test_hybrid_rejects_other_collisions(gpu_lib):
     from plbm import LatticeGrid, PlbmError
     g = LatticeGrid(16, 16, collision="bgki", math="hybrid")
