@@ -41,6 +41,10 @@ struct PluginSim {
   cudaStream_t stream;
   int status;
   unsigned magic_tag;
+  // captured loop of kGraphSteps steps from lattice graph_cur (small grids)
+  cudaGraphExec_t graph;
+  double graph_omega;
+  int graph_cur;
 };
 constexpr unsigned kTag = 0x504c424du;  // "PLBM"
 
@@ -59,22 +63,68 @@ void destroy(PluginSim* s) {
   for (int i = 0; i < 2; i++)
     if (s->f[i]) cudaFree(s->f[i]);
   if (s->scratch) cudaFree(s->scratch);
+  if (s->graph) cudaGraphExecDestroy(s->graph);
   if (s->stream) cudaStreamDestroy(s->stream);
   s->magic_tag = 0;
   delete s;
+}
+
+// One collide-and-push step from lattice `from` to the other.
+cudaError_t push_step(const PluginSim* s, int from, const CollParams& p) {
+  Sweep sw{s->nx, s->ny, s->ld, s->f[from], s->f[1 - from], s->stream};
+  if (s->storage != PLBM_F64) return step_push_dev(s->storage, s->kind, sw, p);
+  if (s->math == PLBM_MATH_STRICT) return strict::step_push_shift_f64(s->kind, sw, p);
+  if (s->math == PLBM_MATH_HYBRID) return step_push_hybrid(s->kind, sw, p);
+  return fma::step_push_shift_f64(s->kind, sw, p);
+}
+
+// Small grids replay a captured loop of kGraphSteps (even) steps instead of
+// launching step by step: their steps are shorter than the host's launch.
+constexpr int kGraphSteps = 16;
+constexpr long long kGraphCells = 1ll << 17;
+
+cudaError_t replay(PluginSim* s, double omega, const CollParams& p, int reps) {
+  if (!s->graph || s->graph_omega != omega || s->graph_cur != s->cur) {
+    if (s->graph) cudaGraphExecDestroy(s->graph);
+    s->graph = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return e;
+    cudaError_t le = cudaSuccess;
+    for (int i = 0; i < kGraphSteps && le == cudaSuccess; i++) le = push_step(s, (s->cur + i) & 1, p);
+    cudaGraph_t graph = nullptr;
+    e = cudaStreamEndCapture(s->stream, &graph);
+    if (le != cudaSuccess || e != cudaSuccess) {
+      if (graph) cudaGraphDestroy(graph);
+      return le != cudaSuccess ? le : e;
+    }
+    e = cudaGraphInstantiate(&s->graph, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+      s->graph = nullptr;
+      return e;
+    }
+    s->graph_omega = omega;
+    s->graph_cur = s->cur;
+  }
+  for (int r = 0; r < reps; r++) {
+    cudaError_t e = cudaGraphLaunch(s->graph, s->stream);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 int do_steps(PluginSim* s, double omega, int nsteps) {
   if (s->status) return s->status;
   if (cudaSetDevice(s->device) != cudaSuccess) return s->status = cuda_fail(cudaGetLastError(), "cudaSetDevice");
   const CollParams p = plbm_make_params(omega, s->trt_magic);
+  if ((long long)s->nx * s->ny <= kGraphCells && nsteps >= 2 * kGraphSteps) {
+    const int reps = nsteps / kGraphSteps;
+    cudaError_t e = replay(s, omega, p, reps);
+    if (e != cudaSuccess) return s->status = cuda_fail(e, "plugin step graph");
+    nsteps -= reps * kGraphSteps;  // even: s->cur unchanged
+  }
   for (int i = 0; i < nsteps; i++) {
-    Sweep sw{s->nx, s->ny, s->ld, s->f[s->cur], s->f[1 - s->cur], s->stream};
-    cudaError_t e;
-    if (s->storage != PLBM_F64) e = step_push_dev(s->storage, s->kind, sw, p);
-    else if (s->math == PLBM_MATH_STRICT) e = strict::step_push_shift_f64(s->kind, sw, p);
-    else if (s->math == PLBM_MATH_HYBRID) e = step_push_hybrid(s->kind, sw, p);
-    else e = fma::step_push_shift_f64(s->kind, sw, p);
+    cudaError_t e = push_step(s, s->cur, p);
     if (e != cudaSuccess) return s->status = cuda_fail(e, "plugin step kernel");
     s->cur = 1 - s->cur;  // move_alloc swap, sim/sim_slbm.F90:114-119
   }

@@ -77,6 +77,27 @@ def test_plugin_steps_equals_repeated_step(gpu_lib):
     b.free()
 
 
+@pytest.mark.parametrize("math,storage", [("strict", "f64"), ("hybrid", "f64"), ("fma", "f32dev")])
+def test_plugin_graph_replay_equals_repeated_step(gpu_lib, math, storage):
+    """c_plbmgpu_steps on a small grid replays a captured loop of steps: the
+    state equals single c_plbmgpu_step calls across odd counts and a change of
+    omega (recapture)."""
+    from plbm.plugin import SimPlugin, make_params
+    p, u = tgv_fields(40, 24)
+    a, b = SimPlugin(), SimPlugin()
+    for s in (a, b):
+        s.init((40, 24), 1.0, p, u, params=make_params(math=math, storage=storage))
+    for n, omega in ((37, 1.5), (50, 1.5), (33, 1.8), (64, 1.8)):
+        for _ in range(n):
+            a.step(omega)
+        b.steps(omega, n)
+        ra, ua = a.vars()
+        rb, ub = b.vars()
+        assert np.array_equal(ra, rb) and np.array_equal(ua, ub)
+    a.free()
+    b.free()
+
+
 def test_tgv_study_convergence_through_plugin(gpu_lib):
     """The reference's TGV study (sim/cases.py:236-330) on this plugin: second-order
     convergence of the L2 velocity error under grid refinement at fixed Re."""
