@@ -205,19 +205,6 @@ DF_HD df64 from_double(double d) {
   return make(hi, lo);
 }
 
-// binary32 -> binary64 bit pattern (exact; binary32 subnormals become 0).
-DF_HD uint64_t float_bits_to_double_bits(float f) {
-  const uint32_t b = f2u(f);
-  const uint32_t ex = (b >> 23) & 0xFFu;
-  if (ex == 0) return (uint64_t)(b & 0x80000000u) << 32;
-  if (ex == 0xFF) return ((uint64_t)(b & 0x80000000u) << 32) | 0x7FF0000000000000ull |
-                         ((uint64_t)(b & 0x7FFFFFu) << 29);
-  const uint64_t hi = (uint64_t)((b & 0x80000000u) | ((ex + 896u) << 20) | ((b & 0x7FFFFFu) >> 3));
-  return (hi << 32) | (uint64_t)((b & 0x7u) << 29);
-}
-
-DF_HD double to_double_exactish(float f) { return u2d(float_bits_to_double_bits(f)); }
-
 // binary32 -> binary64 by bit assembly for finite values (binary32 subnormals
 // become 0); integer instructions only, no conversion on the binary64 pipe.
 DF_HD double f2d_bits(float f) {
@@ -230,46 +217,9 @@ DF_HD double f2d_bits(float f) {
 
 // hi + lo of a normalised pair as one binary64 addition of the exact binary64
 // images of hi and lo (exact whenever lo lies within 29 bits below hi's last
-// bit, as it does after renormalisation).  Costs one binary64 addition where
-// pack_double() costs ~25 integer instructions: the form for kernels whose
-// binary64 pipe has room.
+// bit, as it does after renormalisation): one binary64 addition and a few
+// integer instructions, the form for kernels whose binary64 pipe has room.
 DF_HD double df_to_double(df64 a) { return f2d_bits(a.hi) + f2d_bits(a.lo); }
-
-// hi + lo rounded to binary64 without binary64 arithmetic.  For a
-// normalised pair (|lo| <= ulp(hi)/2) the 53-bit significand of hi + lo is
-// formed in a 64-bit integer: exact when lo reaches at most 29 bits below
-// hi's last bit, otherwise lo is rounded to the binary64 grid of hi
-// (half away from zero) before the add -- an error below 2^-53 |hi + lo|.
-DF_HD double pack_double(df64 a) {
-  const uint32_t bh = f2u(a.hi), bl = f2u(a.lo);
-  const uint32_t exh = (bh >> 23) & 0xFFu;
-  if (exh == 0 || exh == 0xFF) return to_double_exactish(a.hi);
-  const uint32_t exl = (bl >> 23) & 0xFFu;
-  // significand of hi on the binary64 grid: (2^23 + m) * 2^29
-  int64_t M = (int64_t)(0x800000u | (bh & 0x7FFFFFu)) << 29;
-  if (exl != 0) {
-    const int64_t ml = (int64_t)(0x800000u | (bl & 0x7FFFFFu));
-    // lo = ml * 2^(exl-150); grid unit of M is 2^(exh-127-52) => shift = exl - exh + 29
-    const int sh = (int)exl - (int)exh + 29;
-    int64_t li;
-    if (sh >= 0) li = ml << sh;
-    else if (sh > -25) li = (ml + ((int64_t)1 << (-sh - 1))) >> (-sh);
-    else li = 0;
-    if ((bl ^ bh) & 0x80000000u) M -= li;
-    else M += li;
-  }
-  int ex = (int)exh + 896;
-  if (M < ((int64_t)1 << 52)) {  // lo of opposite sign pulled below the binade
-    M <<= 1;
-    ex -= 1;
-  } else if (M >= ((int64_t)1 << 53)) {
-    M = (M + 1) >> 1;
-    ex += 1;
-  }
-  const uint64_t bits = ((uint64_t)(bh & 0x80000000u) << 32) | ((uint64_t)ex << 52) |
-                        ((uint64_t)M & 0xFFFFFFFFFFFFFull);
-  return u2d(bits);
-}
 
 }  // namespace df
 }  // namespace plbm
