@@ -14,6 +14,7 @@
 #include <stdarg.h>
 #include <stdio.h>
 #include <string.h>
+#include <atomic>
 #include <string>
 #include <vector>
 
@@ -24,15 +25,15 @@
 using namespace plbm;
 
 int plbm::block_for(long long cells) {
-  static int sms[64] = {0};
+  static std::atomic<int> sms[64];  // SM count per device, 0 until first asked
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return kBlock;
-  if (!sms[dev]) {
-    int n = 0;
+  int n = sms[dev].load(std::memory_order_relaxed);
+  if (n < 1) {
     if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1) return kBlock;
-    sms[dev] = n;
+    sms[dev].store(n, std::memory_order_relaxed);
   }
-  const long long per_sm = (cells + sms[dev] - 1) / sms[dev];
+  const long long per_sm = (cells + n - 1) / n;
   if (per_sm >= kBlock) return kBlock;
   return (int)(per_sm < 32 ? 32 : (per_sm + 31) / 32 * 32);
 }
@@ -436,7 +437,9 @@ bool graph_key_matches(const plbm_grid_t* g, const void* a, const void* b) {
 
 // Replays the captured loop `reps` times (capturing it first when needed).
 // Returns cudaErrorNotSupported when the stream cannot be captured (the
-// caller's own capture is in progress): the caller then launches step by step.
+// caller's own capture is in progress, or a stream such as the legacy default
+// stream that capture does not take): the caller then launches step by step.
+// Nothing has been launched on the stream when it returns that.
 cudaError_t replay_step_graph(plbm_grid_t* g, const CollParams& p, int reps) {
   void* a = lattice(g, g->iold);
   void* b = lattice(g, g->inew);
@@ -447,8 +450,10 @@ cudaError_t replay_step_graph(plbm_grid_t* g, const CollParams& p, int reps) {
     if (cs != cudaStreamCaptureStatusNone) return cudaErrorNotSupported;
     if (g->step_graph) cudaGraphExecDestroy(g->step_graph);
     g->step_graph = nullptr;
-    e = cudaStreamBeginCapture(g->stream, cudaStreamCaptureModeThreadLocal);
-    if (e != cudaSuccess) return e;
+    if (cudaStreamBeginCapture(g->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+      cudaGetLastError();
+      return cudaErrorNotSupported;
+    }
     cudaError_t le = cudaSuccess;
     for (int i = 0; i < kGraphSteps && le == cudaSuccess; i++)
       le = fused_step(g, i % 2 ? b : a, i % 2 ? a : b, p);

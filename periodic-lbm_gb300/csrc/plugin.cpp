@@ -87,9 +87,12 @@ cudaError_t replay(PluginSim* s, double omega, const CollParams& p, int reps) {
   if (!s->graph || s->graph_omega != omega || s->graph_cur != s->cur) {
     if (s->graph) cudaGraphExecDestroy(s->graph);
     s->graph = nullptr;
-    cudaError_t e = cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal);
-    if (e != cudaSuccess) return e;
+    if (cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+      cudaGetLastError();
+      return cudaErrorNotSupported;  // the caller launches step by step
+    }
     cudaError_t le = cudaSuccess;
+    cudaError_t e;
     for (int i = 0; i < kGraphSteps && le == cudaSuccess; i++) le = push_step(s, (s->cur + i) & 1, p);
     cudaGraph_t graph = nullptr;
     e = cudaStreamEndCapture(s->stream, &graph);
@@ -120,8 +123,8 @@ int do_steps(PluginSim* s, double omega, int nsteps) {
   if ((long long)s->nx * s->ny <= kGraphCells && nsteps >= 2 * kGraphSteps) {
     const int reps = nsteps / kGraphSteps;
     cudaError_t e = replay(s, omega, p, reps);
-    if (e != cudaSuccess) return s->status = cuda_fail(e, "plugin step graph");
-    nsteps -= reps * kGraphSteps;  // even: s->cur unchanged
+    if (e == cudaSuccess) nsteps -= reps * kGraphSteps;  // even: s->cur unchanged
+    else if (e != cudaErrorNotSupported) return s->status = cuda_fail(e, "plugin step graph");
   }
   for (int i = 0; i < nsteps; i++) {
     cudaError_t e = push_step(s, s->cur, p);

@@ -206,6 +206,28 @@ def test_small_grid_graph_replay_equals_single_steps(gpu_lib, math_mode, kind):
         g.close()
 
 
+def test_small_grid_steps_on_torch_default_stream(gpu_lib):
+    """On torch's default stream (cudaStreamLegacy, which stream capture does
+    not take) perform_lbm_step(n) falls back to step-by-step launches."""
+    import torch
+    from plbm import LatticeGrid
+    nx, ny = 40, 24
+    f0 = initial_state(nx, ny, u0=0.03)
+    grids = [LatticeGrid(nx, ny, collision="bgk", math="strict") for _ in range(2)]
+    grids[0].set_stream(torch.cuda.default_stream())
+    for g in grids:
+        g.set_relaxation(1.4, 0.25)
+        g.upload(f0, g.iold)
+    grids[0].perform_lbm_step(48)
+    grids[0].synchronize()
+    for _ in range(48):
+        grids[1].perform_lbm_step(1)
+    a, b = (g.download(g.iold) for g in grids)
+    assert np.array_equal(a[:, :, :ny], b[:, :, :ny])
+    for g in grids:
+        g.close()
+
+
 def test_hybrid_rejects_other_collisions(gpu_lib):
     from plbm import LatticeGrid, PlbmError
     g = LatticeGrid(16, 16, collision="bgki", math="hybrid")
