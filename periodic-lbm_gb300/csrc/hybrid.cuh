@@ -390,6 +390,8 @@ struct TrtParams {
 };
 
 // TRT in the hybrid arithmetic (in place); `bad` and SHIFTED as for bgk_fast.
+// The double-float terms use the lazy operations (no renormalisation; 2 %
+// faster, the same agreement with the oracle).
 template <bool SHIFTED = false>
 DF_HD void trt_fast(double (&f)[9], const TrtParams& p, bool& bad) {
   int64_t F[9];
@@ -399,20 +401,20 @@ DF_HD void trt_fast(double (&f)[9], const TrtParams& p, bool& bad) {
   const int64_t JX = (d57 + d86) + (F[1] - F[3]);
   const int64_t JY = (d57 - d86) + (F[2] - F[4]);
   const df64 jx = fixed_to_df(JX), jy = fixed_to_df(JY);
-  const df64 j2 = df::add(df::sqr(jx), df::sqr(jy));
+  const df64 j2 = df::add_lz(df::sqr_lz(jx), df::sqr_lz(jy));
   {
-    const double c0 = df::df_to_double(df::mul(p.nl0, j2));
+    const double c0 = df::df_to_double(df::mul_lz(p.nl0, j2));
     f[0] = fma_d(p.omb, f[0], fma_d(p.le_t0, lin_to_double<SHIFTED>(R), c0));
   }
-  const df64 c1j2[2] = {df::mul(p.c1[0], j2), df::mul(p.c1[1], j2)};
+  const df64 c1j2[2] = {df::mul_lz(p.c1[0], j2), df::mul_lz(p.c1[1], j2)};
   // MS, MD: the exact brackets of the pair; VDF = c_p.j
 #define PLBM_HY_TRT_PAIR(QP, QM, VDF, MS, MD, A)                                            \
   {                                                                                         \
-    const df64 sym = df::sub(df::mul(p.cs[A], fixed_to_df(MS)),                             \
-                             df::sub(df::mul(p.c4[A], df::sqr(VDF)), c1j2[A]));             \
-    const df64 asym = df::mul(p.cd[A], fixed_to_df(MD));                                    \
-    f[QP] = f[QP] + df::df_to_double(df::neg(df::add(sym, asym)));                          \
-    f[QM] = f[QM] + df::df_to_double(df::sub(asym, sym));                                   \
+    const df64 sym = df::sub_lz(df::mul_lz(p.cs[A], fixed_to_df(MS)),                       \
+                                df::sub_lz(df::mul_lz(p.c4[A], df::sqr_lz(VDF)), c1j2[A])); \
+    const df64 asym = df::mul_lz(p.cd[A], fixed_to_df(MD));                                 \
+    f[QP] = f[QP] + df::df_to_double(df::neg(df::add_lz(sym, asym)));                       \
+    f[QM] = f[QM] + df::df_to_double(df::sub_lz(asym, sym));                                \
   }
   {
     const int64_t s = F[1] + F[3], d = F[1] - F[3];
@@ -424,11 +426,11 @@ DF_HD void trt_fast(double (&f)[9], const TrtParams& p, bool& bad) {
   }
   {
     const int64_t s = F[5] + F[7], d = F[5] - F[7];
-    PLBM_HY_TRT_PAIR(5, 7, df::add(jx, jy), 18 * s - R, 6 * d - (JX + JY), 1)
+    PLBM_HY_TRT_PAIR(5, 7, df::add_lz(jx, jy), 18 * s - R, 6 * d - (JX + JY), 1)
   }
   {
     const int64_t s = F[8] + F[6], d = F[8] - F[6];
-    PLBM_HY_TRT_PAIR(8, 6, df::sub(jx, jy), 18 * s - R, 6 * d - (JX - JY), 1)
+    PLBM_HY_TRT_PAIR(8, 6, df::sub_lz(jx, jy), 18 * s - R, 6 * d - (JX - JY), 1)
   }
 #undef PLBM_HY_TRT_PAIR
 }
