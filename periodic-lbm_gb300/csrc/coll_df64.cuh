@@ -75,10 +75,10 @@ DF_HD void bgk(df64 (&h)[9], const DfParams& p) {
 // no renormalisation, ~44 bits); the nonlinear term
 // omega w rho (4.5 (c.u)^2 - 1.5 u^2), at most ~1e-3, is plain binary32.
 struct DevParams {
-  df64 omb;        // 1 - omega
-  df64 omw[3];     // omega * w  for w0, ws, wd
-  df64 omw3[3];    // 3 omega * w
-  float omwf[3];   // omega * w rounded, for the nonlinear term
+  df64 w[3];     // w0, ws, wd as double-float
+  df64 w3[3];    // 3 w
+  float om_hi;   // omega = om_hi + om_lo
+  float om_lo;
 };
 
 DF_HD df64 add_lazy(df64 a, df64 b) {
@@ -98,6 +98,17 @@ DF_HD df64 mul_lazy_f(df64 a, float b) {
   return p;
 }
 
+// h + omega d rounded once: t = RN(h + om_hi d), its rounding error from one
+// more FMA (h - t is exact, t being close to h), plus om_lo d.  Rounding omega
+// to binary32 instead biased the relaxation rate by ~1e-8, which at
+// tau = 0.52 (viscosity 26x as sensitive as omega) let the shear layer's
+// velocity error grow to 1e-6 over 20,000 steps.
+DF_HD float relax(float h, float d, float om_hi, float om_lo) {
+  const float t = fmaf_(om_hi, d, h);
+  const float c = fmaf_(om_lo, d, fmaf_(om_hi, d, h - t));
+  return t + c;
+}
+
 DF_HD void bgk_dev_comp(float (&h)[9], const DevParams& p) {
   // exact pairwise sums and differences of the stored values
   const df64 s13 = two_sum(h[1], h[3]), s24 = two_sum(h[2], h[4]);
@@ -114,22 +125,24 @@ DF_HD void bgk_dev_comp(float (&h)[9], const DevParams& p) {
   const float ux = jxf * inv, uy = jyf * inv;
   const float rho = 1.0f + dr;
   const float u2 = 1.5f * (ux * ux + uy * uy);
-  // q = 0: h' = (1-w) h0 + omega w0 drho + omega w0 rho (-1.5 u^2)
+  // h' = h + omega (heq - h), heq = w (drho + rho (4.5 (c.u)^2 - 1.5 u^2)) + 3 w c.j.
+  // Only heq needs more than binary32: it is formed in double-float, the
+  // nonlinear term (binary32) joining the exact drho before the product with
+  // w (binary32 weights in that product biased the relaxation rate by ~1e-8);
+  // heq - h is a small difference of nearby values and takes binary32; relax()
+  // adds omega (heq - h) with one rounding, to the storage format.
   {
-    const float nl = p.omwf[0] * (rho * -u2);
-    const df64 v = add_lazy(add_lazy(mul_lazy_f(p.omb, h[0]), mul_lazy(p.omw[0], drho)), make(nl, 0.0f));
-    h[0] = v.hi + v.lo;
+    const df64 e = mul_lazy(p.w[0], add_lazy(drho, make(rho * -u2, 0.0f)));
+    h[0] = relax(h[0], (e.hi - h[0]) + e.lo, p.om_hi, p.om_lo);
   }
 #define PLBM_COMP_PAIR(QP, QM, CUF, CJ, WI)                                              \
   {                                                                                      \
     const float cu = (CUF);                                                              \
-    const float nl = p.omwf[WI] * (rho * fmaf_(4.5f * cu, cu, -u2));                     \
-    const df64 a = add_lazy(mul_lazy(p.omw[WI], drho), make(nl, 0.0f));                  \
-    const df64 b = mul_lazy(p.omw3[WI], CJ);                                             \
-    const df64 vp = add_lazy(add_lazy(mul_lazy_f(p.omb, h[QP]), a), b);                  \
-    const df64 vm = add_lazy(add_lazy(mul_lazy_f(p.omb, h[QM]), a), neg(b));             \
-    h[QP] = vp.hi + vp.lo;                                                               \
-    h[QM] = vm.hi + vm.lo;                                                               \
+    const df64 a = mul_lazy(p.w[WI], add_lazy(drho, make(rho * fmaf_(4.5f * cu, cu, -u2), 0.0f))); \
+    const df64 b = mul_lazy(p.w3[WI], CJ);                                               \
+    const df64 ep = add_lazy(a, b), em = add_lazy(a, neg(b));                            \
+    h[QP] = relax(h[QP], (ep.hi - h[QP]) + ep.lo, p.om_hi, p.om_lo);                     \
+    h[QM] = relax(h[QM], (em.hi - h[QM]) + em.lo, p.om_hi, p.om_lo);                     \
   }
   PLBM_COMP_PAIR(1, 3, ux, jx, 1)
   PLBM_COMP_PAIR(2, 4, uy, jy, 1)

@@ -387,13 +387,13 @@ cudaError_t step_pull_dev_hi(int storage, int math, int kind, const Sweep& s, co
   if (math == 2) {  // compensated binary32
     if (kind != K_BGK) return cudaErrorNotSupported;
     df::DevParams p;
-    p.omb = split_const(cp.omegabar);
     const double w[3] = {W0, WS, WD};
     for (int i = 0; i < 3; i++) {
-      p.omw[i] = split_const(cp.omega * w[i]);
-      p.omw3[i] = split_const(3.0 * cp.omega * w[i]);
-      p.omwf[i] = (float)(cp.omega * w[i]);
+      p.w[i] = split_const(w[i]);
+      p.w3[i] = split_const(3.0 * w[i]);
     }
+    p.om_hi = (float)cp.omega;
+    p.om_lo = (float)(cp.omega - (double)p.om_hi);
     const bool small = (unsigned long long)s.ld * (unsigned long long)s.nx * 9ull < (1ull << 32);
     if (storage == ST_F32DEV) {
       const float* a = static_cast<const float*>(s.src);
