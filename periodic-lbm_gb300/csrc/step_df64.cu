@@ -121,10 +121,9 @@ __device__ __noinline__ void hybrid_fallback_cell(const double* __restrict__ src
 }
 
 // Resident CTAs per SM the hybrid kernels are compiled for (register cap
-// 65536 / (256 x this)): measured best at 8192^2 -- TRT 4 (64 registers, +6 %
-// over the uncapped kernel), BGK and RR 5 (48 registers, +2 to +4 %, a few
-// bytes of spills).
-constexpr int hybrid_min_blocks(int kind) { return kind == K_TRT ? 4 : 5; }
+// 65536 / (256 x this) = 48 registers): measured best at 8192^2 for BGK, TRT
+// and RR alike (4 CTAs: TRT 1 % slower; 6: BGK 2 %, RR 4 % slower).
+constexpr int hybrid_min_blocks(int) { return 5; }
 
 // I: index type of the lattice offsets; 32-bit when the whole lattice has
 // fewer than 2^32 elements (one multiply-add per address instead of 64-bit
