@@ -36,6 +36,12 @@
 // addition: f'_p = f_p + (-sym - asym).  The rest population keeps
 // f'_0 = fma(1 - le, f_0, fma(le 4/9, R, -1.5 le 4/9 |j|^2)).
 //
+// RR (src/collision_regularized.F90:72-194): the non-equilibrium second
+// moments come from exact integer moments (Pxx, Pyy, Pxy), and each population
+// is ONE binary64 FMA, f'_q = fma(w_q, T_q, w_q (rho NL_q + (1 - omega) H_q)),
+// the double-float part formed from six merged Hermite coefficients (rr_fast).
+// TRT and RR use the lazy double-float operations (no renormalisation).
+//
 // Range.  The fast path takes |f_0| < 2, |f_axis| < 1/2, |f_diagonal| < 1/4
 // (biased binary64 exponent at most 1023, 1021, 1020).  Under these limits
 // every integer formed here stays below 16 * 2^59 < 2^63 in magnitude:
