@@ -459,6 +459,33 @@ def test_triple_step_fma_and_plain_steps_interleave(gpu_lib):
     g.close()
 
 
+def test_graph_replay_across_triple_steps_and_kind_changes(gpu_lib):
+    """A small three-lattice grid: replayed step loops (perform_lbm_step(n >= 32))
+    between triple steps, which remap the lattices behind the buffer indices,
+    and across a change of collision kind, equal single steps bit for bit."""
+    from plbm import LatticeGrid
+    nx, ny = 40, 24
+    f0 = initial_state(nx, ny, u0=0.03)
+    grids = [LatticeGrid(nx, ny, nf=3, collision="bgk", math="strict") for _ in range(2)]
+    for g in grids:
+        g.set_relaxation(1.4, 0.25)
+        g.upload(f0, 2)
+    for n, action in ((40, "triple"), (33, "trt"), (48, "triple"), (36, None)):
+        grids[0].perform_lbm_step(n)
+        for _ in range(n):
+            grids[1].perform_lbm_step(1)
+        for g in grids:
+            if action == "triple":
+                g.perform_triple_step(2)
+            elif action:
+                g.collision = action
+        assert grids[0].indices3 == grids[1].indices3
+        a, b = (g.download(g.iold) for g in grids)
+        assert np.array_equal(a[:, :, :ny], b[:, :, :ny])
+    for g in grids:
+        g.close()
+
+
 def test_triple_step_errors(gpu_lib):
     from plbm import LatticeGrid, PlbmError
     g = LatticeGrid(8, 8)  # nf = 2: no imid
