@@ -74,20 +74,15 @@ __device__ __forceinline__ void cell_state(const R (&g)[9], R& rho, R& ux, R& uy
   }
 }
 
-// Block sum: warp sums in the cell arithmetic's type R, the per-warp results
-// converted once and combined in binary64 (one conversion per warp keeps the
-// binary32 kernel off the binary64 pipe).
+// Warp sum in the cell arithmetic's type R (binary32 for deviation storage,
+// keeping the kernel off the binary64 pipe).  Each warp then adds its sum to
+// its own binary64 slot: no block barrier, and the host adds the slots in a
+// fixed order, so the result does not depend on scheduling.
 template <typename R>
-__device__ __forceinline__ double block_sum(R v) {
-  __shared__ double sh[kBlock / 32];
+__device__ __forceinline__ R warp_sum(R v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = (double)v;
-  __syncthreads();
-  double t = 0.0;
-  if (threadIdx.x == 0)
-    for (int i = 0; i < kBlock / 32; i++) t += sh[i];
-  return t;
+  return v;
 }
 
 // f_0 = feq(1, u0) (src/fvm_bardow.F90:99-126 with rho = 1), stored as f or h.
@@ -139,7 +134,7 @@ __global__ void __launch_bounds__(kBlock) k_adj_final(const void* __restrict__ f
 }
 
 // One reverse step: lambda_n from lambda_{n+1} and f_n; adds this step's
-// dL/domega to the block's binary64 slot.  I: offset type (32-bit when the
+// dL/domega to the warp's binary64 slot.  I: offset type (32-bit when the
 // lattice has fewer than 2^32 elements).  The pull sources of the forward
 // step are also where the reverse step scatters mu_p, so one offset table
 // serves the loads of f and the stores of lambda_n.
@@ -191,8 +186,8 @@ __global__ void __launch_bounds__(kBlock) k_adj_step(const void* __restrict__ f,
       lo[off[p]] = (E)mu;
     }
   }
-  const double t = block_sum(part);
-  if (threadIdx.x == 0) dom[blockIdx.x] += t;
+  const R t = warp_sum(part);
+  if ((threadIdx.x & 31) == 0) dom[(size_t)blockIdx.x * (kBlock / 32) + (threadIdx.x >> 5)] += (double)t;
 }
 
 // dL/du0 from lambda_0 and u0.
@@ -244,7 +239,7 @@ cudaError_t dispatch(int what, const AdjLaunch& a) {
 
 }  // namespace
 
-int adjoint_blocks(int nx, int ny) { return tiles(ny) * nx; }
+int adjoint_blocks(int nx, int ny) { return tiles(ny) * nx * (kBlock / 32); }
 
 cudaError_t adjoint_launch(int storage, int what, const AdjLaunch& a) {
   if (storage == ST_F64) return dispatch<ST_F64>(what, a);

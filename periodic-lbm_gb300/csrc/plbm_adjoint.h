@@ -20,6 +20,7 @@ struct AdjLaunch {
 // what: 0 init f_0 into a.f (cast away const), 1 final (u_T -> out, lambda_T -> lam_out),
 //       2 reverse step, 3 dL/du0.
 cudaError_t adjoint_launch(int storage, int what, const AdjLaunch& a);
+// binary64 slots for dL/domega (one per warp of the reverse-step launch)
 int adjoint_blocks(int nx, int ny);
 
 }  // namespace plbm
