@@ -340,7 +340,10 @@ __device__ __forceinline__ void coll_bgk_shift(R (&f)[9], R omega) {
 // With v = h + w, the constant parts cancel exactly:
 //   v_a + v_b - t*feq_common = h_a + h_b - t*(drho - 1.5 j^2),  v_a - v_b = h_a - h_b,
 // so the operator is the reference's with h for v and drho for rho.
-template <typename R>
+// SC: populations held scaled by 2^15 (binary16 storage); the operator is
+// linear in them except for its squares of j, which take one factor 2^-15
+// (q = 2^-15 j is the second factor of each).
+template <typename R, bool SC = false>
 __device__ __forceinline__ void coll_trt_shift(R (&v)[9], R le, R les, R lds) {
   const R t0 = R(4) / R(9), t1x2 = R(2) / R(9), t2x2 = R(2) / R(36);
   const R fac1 = t1x2 * R(4.5), fac2 = t2x2 * R(4.5);
@@ -349,16 +352,21 @@ __device__ __forceinline__ void coll_trt_shift(R (&v)[9], R le, R les, R lds) {
   R drho = (((vNE + vSW) + (vNW + vSE)) + ((vE + vW) + (vN + vS))) + vC;
   R velX = (((vNE - vSW) + (vSE - vNW)) + (vE - vW));
   R velY = (((vNE - vSW) + (vNW - vSE)) + (vN - vS));
-  R velX2 = velX * velX, velY2 = velY * velY;
+  R qx = velX, qy = velY;
+  if constexpr (SC) {
+    qx = velX * R(1.0 / 32768.0);
+    qy = velY * R(1.0 / 32768.0);
+  }
+  R velX2 = velX * qx, velY2 = velY * qy;
   R fc = drho - R(1.5) * (velX2 + velY2);
   v[0] = vC * (R(1) - le) + le * t0 * fc;
   R velXPY = velX + velY;
-  R sym = les * (vNE + vSW - fac2 * velXPY * velXPY - t2x2 * fc);
+  R sym = les * (vNE + vSW - fac2 * velXPY * (qx + qy) - t2x2 * fc);
   R asym = lds * (vNE - vSW - R(3) * t2x2 * velXPY);
   v[5] = vNE - sym - asym;
   v[7] = vSW - sym + asym;
   R velXMY = velX - velY;
-  sym = les * (vSE + vNW - fac2 * velXMY * velXMY - t2x2 * fc);
+  sym = les * (vSE + vNW - fac2 * velXMY * (qx - qy) - t2x2 * fc);
   asym = lds * (vSE - vNW - R(3) * t2x2 * velXMY);
   v[8] = vSE - sym - asym;
   v[6] = vNW - sym + asym;
@@ -376,19 +384,30 @@ __device__ __forceinline__ void coll_trt_shift(R (&v)[9], R le, R les, R lds) {
 // shifted populations.  The equilibrium is split as feq_i = w_i*(rho + rho*P_i)
 // with P_i the velocity polynomial, so heq_i = feq_i - w_i = w_i*(drho + rho*P_i);
 // non-equilibrium parts h_i - heq_i equal f_i - feq_i exactly in real arithmetic.
-template <typename R>
+// SC: populations held scaled by S = 2^15 (binary16 storage); the operator is
+// linear in them except through rho and u: rho = 1 + drho/S, u = j/(S rho),
+// and heq scaled is w*(drho + S rho P).  SC is binary32 only: 1/rho takes the
+// approximate division (2 ulp), far below the storage's 2^-11 rounding.
+template <typename R, bool SC = false>
 __device__ __forceinline__ void coll_rr_shift(R (&f)[9], R rr_w0, R rr_ws, R rr_wd) {
   const R w0 = R(4) / R(9), ws = R(1) / R(9), wd = R(1) / R(36), csqr = R(1) / R(3);
   R vC = f[0], vE = f[1], vN = f[2], vW = f[3], vS = f[4];
   R vNE = f[5], vNW = f[6], vSW = f[7], vSE = f[8];
   R drho = (((vNE + vSW) + (vNW + vSE)) + ((vE + vW) + (vN + vS))) + vC;
-  R rho = drho + R(1);
-  R invrho = R(1) / rho;
+  R rho, invrho;
+  if constexpr (SC) {
+    rho = drho * R(1.0 / 32768.0) + R(1);
+    invrho = __fdividef(R(1.0 / 32768.0), rho);
+  } else {
+    rho = drho + R(1);
+    invrho = R(1) / rho;
+  }
   R ux = invrho * (((vNE - vSW) + (vSE - vNW)) + (vE - vW));
   R uy = invrho * (((vNE - vSW) + (vNW - vSE)) + (vN - vS));
   R uxx = ux * ux, uyy = uy * uy;
   R uxxy = uxx * uy, uyyx = uyy * ux, uxxyy = uxx * uyy;
   // P terms: indp0 - 1 etc.
+  if constexpr (SC) rho = rho * R(32768);
   R p0 = R(-1.5) * (uxx + uyy);
   R ps = p0 - R(4.5) * uxxyy;
   R pd = p0 + R(9) * uxxyy;

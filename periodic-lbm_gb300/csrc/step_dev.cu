@@ -4,6 +4,8 @@
 // sim/sim.F90:131,384) in binary32 or in binary16 scaled by 2^15, and the
 // collision runs in binary32 on the shifted form (coll_*_shift).  The
 // traffic per cell update is 72 B (binary32) or 36 B (binary16).
+#include <type_traits>
+
 #include "plbm_launch.h"
 
 namespace plbm {
@@ -55,6 +57,38 @@ ShiftParamsF shift_params(int kind, const CollParams& p) {
   return {(float)p.omega, 0.0f, 0.0f};
 }
 
+// BGK on binary16 deviations kept in their stored scale, H = 2^15 h: the
+// scale enters the constants instead of 18 multiplies per cell.  rho = 1 +
+// 2^-15 sum H, u = j / rho, and H' = (1 - omega) H + omega Heq with Heq =
+// w (sum H + 2^15 rho P), P = -1.5 u^2 + 3 c.u + 4.5 (c.u)^2 -- the shifted
+// equilibrium of coll_bgk_shift, scaled, with omega w folded into the two
+// per-cell factors.  u takes the approximate division (2 ulp): binary16
+// storage rounds the populations to 2^-11 relative, far above it.
+__device__ __forceinline__ void coll_bgk_shift_f16scaled(float (&H)[9], float omega) {
+  const float dh = (((H[5] + H[7]) + (H[6] + H[8])) + ((H[1] + H[3]) + (H[2] + H[4]))) + H[0];
+  const float rho = fmaf(dh, F16_INV_SCALE, 1.0f);
+  const float r = __fdividef(F16_INV_SCALE, rho);
+  const float ux = (((H[5] - H[7]) + (H[8] - H[6])) + (H[1] - H[3])) * r;
+  const float uy = (((H[5] - H[7]) + (H[6] - H[8])) + (H[2] - H[4])) * r;
+  const float uxx = ux * ux, uyy = uy * uy;
+  const float indp = -1.5f * (uxx + uyy);
+  const float sr = F16_SCALE * rho, omb = 1.0f - omega;
+  const float a0 = omega * (4.0f / 9.0f), as = omega * (1.0f / 9.0f), ad = omega * (1.0f / 36.0f);
+  const float k00 = a0 * dh, k10 = a0 * sr, k0s = as * dh, k1s = as * sr, k0d = ad * dh, k1d = ad * sr;
+  H[0] = fmaf(omb, H[0], fmaf(k10, indp, k00));
+  const float bx = fmaf(4.5f, uxx, indp), by = fmaf(4.5f, uyy, indp);
+  H[1] = fmaf(omb, H[1], fmaf(k1s, fmaf(3.0f, ux, bx), k0s));
+  H[3] = fmaf(omb, H[3], fmaf(k1s, fmaf(-3.0f, ux, bx), k0s));
+  H[2] = fmaf(omb, H[2], fmaf(k1s, fmaf(3.0f, uy, by), k0s));
+  H[4] = fmaf(omb, H[4], fmaf(k1s, fmaf(-3.0f, uy, by), k0s));
+  const float uxpy = ux + uy, uxmy = ux - uy;
+  const float bp = fmaf(4.5f * uxpy, uxpy, indp), bm = fmaf(4.5f * uxmy, uxmy, indp);
+  H[5] = fmaf(omb, H[5], fmaf(k1d, fmaf(3.0f, uxpy, bp), k0d));
+  H[7] = fmaf(omb, H[7], fmaf(k1d, fmaf(-3.0f, uxpy, bp), k0d));
+  H[6] = fmaf(omb, H[6], fmaf(k1d, fmaf(-3.0f, uxmy, bm), k0d));
+  H[8] = fmaf(omb, H[8], fmaf(k1d, fmaf(3.0f, uxmy, bm), k0d));
+}
+
 // The pull step of the src/ layout (YFast) with explicit pull offsets: I is
 // the offset type, 32-bit when the lattice has fewer than 2^32 elements (one
 // multiply-add per address instead of 64-bit index arithmetic).
@@ -68,20 +102,26 @@ __global__ void __launch_bounds__(kBlock) k_step_dev_pull(const typename S::elem
   const I L = (I)ld, P = (I)ld * (I)nx;
   const I c0 = (I)x * L, cm = (I)wrap_m(x, nx) * L, cp = (I)wrap_p(x, nx) * L;
   const I y0 = (I)y, ym = (I)wrap_m(y, ny), yp = (I)wrap_p(y, ny);
+  const I offs[9] = {c0 + y0,         P + cm + y0,     2 * P + c0 + ym, 3 * P + cp + y0, 4 * P + c0 + yp,
+                     5 * P + cm + ym, 6 * P + cp + ym, 7 * P + cp + yp, 8 * P + cm + yp};
+  const I o = c0 + y0;
+  if constexpr (std::is_same<S, StoreF16Dev>::value) {
+    float H[9];
+#pragma unroll
+    for (int q = 0; q < 9; q++) H[q] = __half2float(__ldg(src + offs[q]));
+    if constexpr (KIND == K_TRT) coll_trt_shift<float, true>(H, p.a, p.b, p.c);
+    else if constexpr (KIND == K_RR) coll_rr_shift<float, true>(H, p.a, p.b, p.c);
+    else coll_bgk_shift_f16scaled(H, p.a);
+#pragma unroll
+    for (int q = 0; q < 9; q++) dst[(I)q * P + o] = __float2half_rn(H[q]);
+    return;
+  }
   float h[9];
-  h[0] = S::load(src, c0 + y0);
-  h[1] = S::load(src, P + cm + y0);
-  h[2] = S::load(src, 2 * P + c0 + ym);
-  h[3] = S::load(src, 3 * P + cp + y0);
-  h[4] = S::load(src, 4 * P + c0 + yp);
-  h[5] = S::load(src, 5 * P + cm + ym);
-  h[6] = S::load(src, 6 * P + cp + ym);
-  h[7] = S::load(src, 7 * P + cp + yp);
-  h[8] = S::load(src, 8 * P + cm + yp);
+#pragma unroll
+  for (int q = 0; q < 9; q++) h[q] = S::load(src, offs[q]);
   if (KIND == K_TRT) coll_trt_shift<float>(h, p.a, p.b, p.c);
   else if (KIND == K_RR) coll_rr_shift<float>(h, p.a, p.b, p.c);
   else coll_bgk_shift<float>(h, p.a);
-  const I o = c0 + y0;
 #pragma unroll
   for (int q = 0; q < 9; q++) S::store(dst, (I)q * P + o, h[q]);
 }
