@@ -126,6 +126,47 @@ __global__ void __launch_bounds__(kBlock) k_step_dev_pull(const typename S::elem
   for (int q = 0; q < 9; q++) S::store(dst, (I)q * P + o, h[q]);
 }
 
+// The binary16 pull step with two y-adjacent cells per thread (y even): the
+// nine stores and the three loads without a y shift move as half2, one
+// 4-byte access and one conversion for both cells.  The cell operations are
+// those of k_step_dev_pull<StoreF16Dev>.  Needs ny even (y + 1 < ny), ld even
+// and 4-byte aligned lattices, so that every half2 offset is even.
+template <int KIND, typename I>
+__global__ void __launch_bounds__(kBlock) k_step_f16_pull2(const __half* __restrict__ src, __half* __restrict__ dst,
+                                                          int nx, int ny, int ld, int ftiles, ShiftParamsF p) {
+  const int x = blockIdx.x / ftiles;
+  const int y = 2 * ((blockIdx.x - x * ftiles) * blockDim.x + threadIdx.x);
+  if (y >= ny) return;
+  const I L = (I)ld, P = (I)ld * (I)nx;
+  const I c0 = (I)x * L, cm = (I)wrap_m(x, nx) * L, cp = (I)wrap_p(x, nx) * L;
+  const I y0 = (I)y, y1 = (I)(y + 1), ym = (I)wrap_m(y, ny), yp = (I)wrap_p(y + 1, ny);
+  const __half2* s2 = reinterpret_cast<const __half2*>(src);
+  float A[9], B[9];
+  const float2 v0 = __half22float2(__ldg(s2 + (c0 + y0) / 2));
+  const float2 v1 = __half22float2(__ldg(s2 + (P + cm + y0) / 2));
+  const float2 v3 = __half22float2(__ldg(s2 + (3 * P + cp + y0) / 2));
+  A[0] = v0.x, B[0] = v0.y, A[1] = v1.x, B[1] = v1.y, A[3] = v3.x, B[3] = v3.y;
+  A[2] = __half2float(__ldg(src + 2 * P + c0 + ym)), B[2] = __half2float(__ldg(src + 2 * P + c0 + y0));
+  A[4] = __half2float(__ldg(src + 4 * P + c0 + y1)), B[4] = __half2float(__ldg(src + 4 * P + c0 + yp));
+  A[5] = __half2float(__ldg(src + 5 * P + cm + ym)), B[5] = __half2float(__ldg(src + 5 * P + cm + y0));
+  A[6] = __half2float(__ldg(src + 6 * P + cp + ym)), B[6] = __half2float(__ldg(src + 6 * P + cp + y0));
+  A[7] = __half2float(__ldg(src + 7 * P + cp + y1)), B[7] = __half2float(__ldg(src + 7 * P + cp + yp));
+  A[8] = __half2float(__ldg(src + 8 * P + cm + y1)), B[8] = __half2float(__ldg(src + 8 * P + cm + yp));
+  if constexpr (KIND == K_TRT) {
+    coll_trt_shift<float, true>(A, p.a, p.b, p.c);
+    coll_trt_shift<float, true>(B, p.a, p.b, p.c);
+  } else if constexpr (KIND == K_RR) {
+    coll_rr_shift<float, true>(A, p.a, p.b, p.c);
+    coll_rr_shift<float, true>(B, p.a, p.b, p.c);
+  } else {
+    coll_bgk_shift_f16scaled(A, p.a);
+    coll_bgk_shift_f16scaled(B, p.a);
+  }
+  __half2* d2 = reinterpret_cast<__half2*>(dst) + (c0 + y0) / 2;
+#pragma unroll
+  for (int q = 0; q < 9; q++) d2[(I)q * (P / 2)] = __floats2half2_rn(A[q], B[q]);
+}
+
 template <class S>
 __global__ void __launch_bounds__(kBlock) k_stream_dev(const typename S::elem* __restrict__ src,
                                                       typename S::elem* __restrict__ dst, int nx, int ny,
@@ -211,10 +252,33 @@ cudaError_t launch_pull_dev(int kind, const Sweep& s, const CollParams& cp) {
   return cudaGetLastError();
 }
 
+template <typename I>
+cudaError_t launch_f16_pull2(int kind, const Sweep& s, const CollParams& cp) {
+  const int bs = block_for((long long)s.nx * (s.ny / 2));
+  const int ft = (s.ny / 2 + bs - 1) / bs;
+  const long long blocks = (long long)ft * s.nx;
+  if (blocks <= 0 || blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+  const __half* a = static_cast<const __half*>(s.src);
+  __half* b = static_cast<__half*>(s.dst);
+  const ShiftParamsF p = shift_params(kind, cp);
+  const unsigned nb = (unsigned)blocks;
+  switch (kind) {
+    case K_BGK: k_step_f16_pull2<K_BGK, I><<<nb, bs, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft, p); break;
+    case K_TRT: k_step_f16_pull2<K_TRT, I><<<nb, bs, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft, p); break;
+    case K_RR: k_step_f16_pull2<K_RR, I><<<nb, bs, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft, p); break;
+    default: return cudaErrorNotSupported;
+  }
+  return cudaGetLastError();
+}
+
 }  // namespace
 
 cudaError_t step_pull_dev(int storage, int kind, const Sweep& s, const CollParams& p) {
   const bool small = (unsigned long long)s.ld * (unsigned long long)s.nx * 9ull < (1ull << 32);
+  const bool pairs = s.ny % 2 == 0 && s.ld % 2 == 0 &&
+                     (((uintptr_t)s.src | (uintptr_t)s.dst) & 3) == 0;
+  if (storage == ST_F16DEV && pairs)
+    return small ? launch_f16_pull2<uint32_t>(kind, s, p) : launch_f16_pull2<size_t>(kind, s, p);
   if (storage == ST_F32DEV)
     return small ? launch_pull_dev<StoreF32Dev, uint32_t>(kind, s, p) : launch_pull_dev<StoreF32Dev, size_t>(kind, s, p);
   if (storage == ST_F16DEV)
