@@ -2,7 +2,9 @@
 //
 // Populations are held as h_i = f_i - w_i (the shifted form of
 // sim/sim.F90:131,384) in binary32 or in binary16 scaled by 2^15, and the
-// collision runs in binary32 on the shifted form (coll_*_shift).  The
+// collision runs in binary32 on the shifted form (coll_*_shift).  The fused
+// binary16 pull step collides in the stored scale (H = 2^15 h) and, on even
+// ny, updates two y-adjacent cells per thread (k_step_f16_pull2).  The
 // traffic per cell update is 72 B (binary32) or 36 B (binary16).
 #include <type_traits>
 
