@@ -131,6 +131,7 @@ int read_npy_header(FILE* fp, const char* path, NpyInfo* info) {
     long long v = 0;
     bool any = false;
     while (i < sh.size() - 1 && sh[i] >= '0' && sh[i] <= '9') {
+      if (v > (1LL << 53)) return fail(PLBM_E_INVALID, "%s: extent too large in shape %s", path, sh.c_str());
       v = v * 10 + (sh[i] - '0');
       any = true;
       i++;

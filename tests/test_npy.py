@@ -50,3 +50,58 @@ def test_rejects_other_dtypes_and_garbage(lattice, tmp_path):
         lattice.read_npy_header(q)
     with pytest.raises(PlbmError):
         lattice.read_npy_header(tmp_path / "missing.npy")
+
+
+def _raw_npy(path, header: str, version=(1, 0), data=b""):
+    h = header.encode()
+    pad = 64 - (len(h) + 11) % 64
+    h = h + b" " * pad + b"\n"
+    pre = b"\x93NUMPY" + bytes(version)
+    pre += len(h).to_bytes(2 if version[0] == 1 else 4, "little")
+    path.write_bytes(pre + h + data)
+
+
+@pytest.mark.parametrize("header", [
+    "{'descr': '<f8', 'fortran_order': False, 'shape': (99999999999999999999999, 2), }",
+    "{'descr': '<f8', 'fortran_order': False, 'shape': (1, 2, 3, 4, 5, 6, 7, 8, 9), }",
+    "{'descr': '<f8', 'fortran_order': False, 'shape': (3, -4), }",
+    "{'descr': '<f8', 'fortran_order': Maybe, 'shape': (3,), }",
+    "{'descr': '<f8', 'fortran_order': False, 'shape': 3, }",
+    "{'descr': '<f8', 'fortran_order': False, }",
+    "{'descr': '>f8', 'fortran_order': False, 'shape': (3,), }",
+])
+def test_rejects_malformed_headers(lattice, tmp_path, header):
+    from plbm import PlbmError
+    p = tmp_path / "m.npy"
+    _raw_npy(p, header)
+    with pytest.raises(PlbmError):
+        lattice.read_npy_header(p)
+
+
+def test_truncated_header_and_other_versions(lattice, tmp_path):
+    from plbm import PlbmError
+    p = tmp_path / "t.npy"
+    _raw_npy(p, "{'descr': '<f8', 'fortran_order': True, 'shape': (3, 4), }")
+    p.write_bytes(p.read_bytes()[:30])
+    with pytest.raises(PlbmError):
+        lattice.read_npy_header(p)
+    q = tmp_path / "v2.npy"
+    _raw_npy(q, "{'descr': '<f8', 'fortran_order': True, 'shape': (3, 4), }", version=(2, 0))
+    h = lattice.read_npy_header(q)
+    assert h["shape"] == (3, 4) and h["fortran_order"] and h["data_offset"] == q.stat().st_size
+    r = tmp_path / "v9.npy"
+    _raw_npy(r, "{'descr': '<f8', 'fortran_order': True, 'shape': (3, 4), }", version=(9, 0))
+    with pytest.raises(PlbmError):
+        lattice.read_npy_header(r)
+
+
+def test_reads_numpy_version2_and_scalar_headers(lattice, tmp_path):
+    p = tmp_path / "v2np.npy"
+    a = np.arange(6.0).reshape(2, 3)
+    with open(p, "wb") as fh:
+        np.lib.format.write_array(fh, a, version=(2, 0))
+    h = lattice.read_npy_header(p)
+    assert h["shape"] == (2, 3) and not h["fortran_order"] and h["data_offset"] == p.stat().st_size - a.nbytes
+    s = tmp_path / "s.npy"
+    np.save(s, np.float64(2.5))
+    assert lattice.read_npy_header(s)["shape"] == ()
