@@ -30,6 +30,11 @@ extern "C" {
 #define PLBM_E_TIMEOUT     -5  /* a bounded device-side wait expired        */
 #define PLBM_E_NODEVICE    -6  /* no CUDA device visible                    */
 
+/* Largest nx, ny (and ld) accepted: the kernels index cells with 32-bit
+ * coordinates, which must not overflow when rounded up to a whole tile.
+ * Larger extents are rejected with PLBM_E_INVALID. */
+#define PLBM_MAX_EXTENT (1 << 30)
+
 /* ---- collision kinds (grid%collision => collide_*) ---------------------- */
 #define PLBM_BGK   0  /* collide_bgk, src/collision_bgk.F90:17-82          */
 #define PLBM_TRT   1  /* collide_trt, src/collision_trt.F90:41-160         */

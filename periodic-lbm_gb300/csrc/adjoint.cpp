@@ -77,7 +77,7 @@ extern "C" int plbm_adjoint_create(int nx, int ny, int storage, int nsteps, int 
                                    plbm_adjoint_t** out) {
   if (!out) return fail(PLBM_E_INVALID, "out is NULL");
   *out = nullptr;
-  if (nx < 1 || ny < 1 || nsteps < 1 || checkpoint_every < 1)
+  if (nx < 1 || ny < 1 || nx > PLBM_MAX_EXTENT || ny > PLBM_MAX_EXTENT || nsteps < 1 || checkpoint_every < 1)
     return fail(PLBM_E_INVALID, "bad adjoint sizes nx=%d ny=%d nsteps=%d checkpoint_every=%d", nx, ny, nsteps,
                 checkpoint_every);
   if (storage != PLBM_F64 && storage != PLBM_F32DEV)

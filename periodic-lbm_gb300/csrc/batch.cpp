@@ -197,6 +197,11 @@ extern "C" int plbm_batch_create(int ngrids, const int* nx, const int* ny, const
   if (ngrids < 1 || !nx || !ny || !kind || !omega) return fail(PLBM_E_INVALID, "bad batch description");
   if (storage != PLBM_F64 && storage != PLBM_F32DEV)
     return fail(PLBM_E_UNSUPPORTED, "batched storage %d (PLBM_F64 or PLBM_F32DEV)", storage);
+  for (int i = 0; i < ngrids; i++)
+    if (nx[i] < 1 || ny[i] < 1 || nx[i] > PLBM_MAX_EXTENT || ny[i] > PLBM_MAX_EXTENT ||
+        (kind[i] != PLBM_BGK && kind[i] != PLBM_TRT) || !(omega[i] > 0 && omega[i] < 2))
+      return fail(PLBM_E_INVALID, "grid %d: nx=%d ny=%d kind=%d omega=%g (BGK or TRT, 0<omega<2)", i, nx[i], ny[i],
+                  kind[i], omega[i]);
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
     cudaGetLastError();
@@ -211,11 +216,6 @@ extern "C" int plbm_batch_create(int ngrids, const int* nx, const int* ny, const
   b->grids.resize(ngrids);
   size_t off = 0;
   for (int i = 0; i < ngrids; i++) {
-    if (nx[i] < 1 || ny[i] < 1 || (kind[i] != PLBM_BGK && kind[i] != PLBM_TRT) || !(omega[i] > 0 && omega[i] < 2)) {
-      delete b;
-      return fail(PLBM_E_INVALID, "grid %d: nx=%d ny=%d kind=%d omega=%g (BGK or TRT, 0<omega<2)", i, nx[i], ny[i],
-                  kind[i], omega[i]);
-    }
     BatchGrid& g = b->grids[i];
     memset(&g, 0, sizeof g);
     g.nx = nx[i];

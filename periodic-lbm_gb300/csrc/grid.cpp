@@ -89,6 +89,8 @@ extern "C" int plbm_grid_create(int nx, int ny, int nf, int storage, plbm_grid_t
   if (!out) return fail(PLBM_E_INVALID, "out is NULL");
   *out = nullptr;
   if (nx < 1 || ny < 1) return fail(PLBM_E_INVALID, "grid size %dx%d: nx and ny must be >= 1", nx, ny);
+  if (nx > PLBM_MAX_EXTENT || ny > PLBM_MAX_EXTENT)
+    return fail(PLBM_E_INVALID, "grid size %dx%d: nx and ny must be <= %d", nx, ny, PLBM_MAX_EXTENT);
   if (nf < 2 || nf > 16) return fail(PLBM_E_INVALID, "nf = %d: need 2 <= nf <= 16", nf);
   if (storage != PLBM_F64 && storage != PLBM_F32DEV && storage != PLBM_F16DEV)
     return fail(PLBM_E_INVALID, "unknown storage %d", storage);
@@ -595,7 +597,8 @@ extern "C" int plbm_update_macros(plbm_grid_t* g, double* rho, double* ux, doubl
 
 extern "C" int plbm_vorticity_device(int order, int nx, int ny, const double* ux, const double* uy, double* w,
                                      void* stream) {
-  if (nx < 1 || ny < 1) return fail(PLBM_E_INVALID, "grid size %dx%d", nx, ny);
+  if (nx < 1 || ny < 1 || nx > PLBM_MAX_EXTENT || ny > PLBM_MAX_EXTENT)
+    return fail(PLBM_E_INVALID, "grid size %dx%d", nx, ny);
   if (order != 2 && order != 4 && order != 44) return fail(PLBM_E_INVALID, "vorticity order %d (2, 4 or 44)", order);
   if (!ux || !uy || !w) return fail(PLBM_E_INVALID, "NULL field");
   CUDA_TRY(vorticity(order, nx, ny, ux, uy, w, static_cast<cudaStream_t>(stream)), "vorticity kernel");
@@ -603,7 +606,8 @@ extern "C" int plbm_vorticity_device(int order, int nx, int ny, const double* ux
 }
 
 extern "C" int plbm_vorticity(int order, int nx, int ny, const double* ux, const double* uy, double* w) {
-  if (nx < 1 || ny < 1) return fail(PLBM_E_INVALID, "grid size %dx%d", nx, ny);
+  if (nx < 1 || ny < 1 || nx > PLBM_MAX_EXTENT || ny > PLBM_MAX_EXTENT)
+    return fail(PLBM_E_INVALID, "grid size %dx%d", nx, ny);
   if (order != 2 && order != 4 && order != 44) return fail(PLBM_E_INVALID, "vorticity order %d (2, 4 or 44)", order);
   if (!ux || !uy || !w) return fail(PLBM_E_INVALID, "NULL field");
   int ndev = 0;
@@ -690,7 +694,8 @@ extern "C" int plbm_hybrid_range_flag(int* flag, int reset) {
 
 extern "C" int plbm_launch_step(int storage, int math, int kind, int nx, int ny, int ld, const void* fsrc,
                                 void* fdst, double omega, double trt_magic, void* stream) {
-  if (nx < 1 || ny < 1 || ld < ny) return fail(PLBM_E_INVALID, "bad sizes nx=%d ny=%d ld=%d", nx, ny, ld);
+  if (nx < 1 || ny < 1 || ld < ny || nx > PLBM_MAX_EXTENT || ld > PLBM_MAX_EXTENT)
+    return fail(PLBM_E_INVALID, "bad sizes nx=%d ny=%d ld=%d", nx, ny, ld);
   if (!fsrc || !fdst || fsrc == fdst) return fail(PLBM_E_INVALID, "fsrc and fdst must be distinct device lattices");
   if (kind < PLBM_BGK || kind > PLBM_BGKI) return fail(PLBM_E_INVALID, "unknown collision kind %d", kind);
   const CollParams p = plbm_make_params(omega, trt_magic);

@@ -138,7 +138,7 @@ int do_steps(PluginSim* s, double omega, int nsteps) {
 
 extern "C" void* c_plbmgpu_init(int nx, int ny, double dt, const double* rho, const double* u,
                                 const double* sigma, void* params) {
-  if (nx < 1 || ny < 1) {
+  if (nx < 1 || ny < 1 || nx > PLBM_MAX_EXTENT || ny > PLBM_MAX_EXTENT) {
     fail(PLBM_E_INVALID, "grid size %dx%d", nx, ny);
     return nullptr;
   }

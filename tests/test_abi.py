@@ -66,6 +66,31 @@ def test_invalid_arguments_are_rejected_without_a_device(lib):
     assert lib.plbm_launch_step(0, 0, 0, 8, 8, 4, None, None, 1.0, 0.25, None) == _lib.PLBM_E_INVALID
 
 
+def test_extents_above_the_32_bit_cell_limit_are_rejected(lib):
+    """PLBM_MAX_EXTENT (2^30) bounds nx, ny and ld at every entry point that
+    takes grid sizes, before any device work: the kernels' 32-bit cell
+    coordinates, rounded up to whole tiles, must not overflow."""
+    from plbm import _lib
+    big = (1 << 30) + 1
+    h = C.c_void_p()
+    for nx, ny in ((big, 8), (8, big)):
+        assert lib.plbm_grid_create(nx, ny, 2, 2, C.byref(h)) == _lib.PLBM_E_INVALID
+        assert "<= 1073741824" in _lib.last_error()
+        assert lib.plbm_vorticity(2, nx, ny, None, None, None) == _lib.PLBM_E_INVALID
+        assert "grid size" in _lib.last_error()
+        assert lib.plbm_adjoint_create(nx, ny, 0, 10, 3, C.byref(h)) == _lib.PLBM_E_INVALID
+        p = np.zeros(1)
+        assert not lib.c_plbmgpu_init(nx, ny, 1.0, p.ctypes.data, p.ctypes.data, None, None)
+        assert "grid size" in _lib.last_error()
+        nxa, nya = (C.c_int * 1)(nx), (C.c_int * 1)(ny)
+        kind, om = (C.c_int * 1)(0), (C.c_double * 1)(1.0)
+        assert lib.plbm_batch_create(1, nxa, nya, kind, om, None, 0, C.byref(h)) == _lib.PLBM_E_INVALID
+    assert lib.plbm_launch_step(0, 0, 0, 8, 8, big, C.c_void_p(16), C.c_void_p(32), 1.0, 0.25,
+                                None) == _lib.PLBM_E_INVALID
+    assert "bad sizes" in _lib.last_error()
+    assert "#define PLBM_MAX_EXTENT (1 << 30)" in (ROOT / "include" / "plbm_gpu.h").read_text()
+
+
 def test_create_without_device_reports_nodevice_or_succeeds(lib):
     from plbm import _lib
     h = C.c_void_p()
