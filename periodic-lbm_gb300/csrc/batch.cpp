@@ -223,7 +223,7 @@ extern "C" int plbm_batch_create(int ngrids, const int* nx, const int* ny, const
     g.ld = pad16(ny[i]);
     g.kind = kind[i];
     g.p = plbm_make_params(omega[i], trt_magic ? trt_magic[i] : 0.25);
-    g.hp = hybrid_params(omega[i]);
+    g.hp = hybrid_bgk_params(omega[i]);
     g.ht = hybrid_trt_params(g.p);
     g.off = (long long)off;
     off += 2 * (size_t)g.ld * g.nx * 9;

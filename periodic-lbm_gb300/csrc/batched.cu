@@ -110,7 +110,7 @@ __device__ __forceinline__ void do_tile(const BatchGrid* __restrict__ gp, int2 x
     if (HY > 0 || (HY < 0 && __ldg(&gp->hybrid))) {
       bool bad = false;
       if (kind == K_TRT) hy::trt_fast(f, gp->ht, bad);
-      else hy::bgk_fast(f, gp->hp, bad);
+      else hy::bgk_fma(f, gp->hp, bad);
       if (bad) {  // outside the hybrid range: the binary64 operator on the same inputs
         fallback_cell<CG>(src, dst, x, y, gp);
         return;

@@ -12,16 +12,21 @@
 //   R, JX, JY = sum F_q, sum cx F_q, sum cy F_q          exact integer sums
 //
 // BGK (src/collision_bgk.F90:58-71, equilibrium src/fvm_bardow.F90:99-126):
-//   C_q      = rho (4.5 (c_q.u)^2 - 1.5 u^2)             double-float, |C| <~ 1e-2
-//   T_q      = R + 3 c_q.J + C_q                         integer (C_q's two
+//   populations (bgk_fma): f'_q = fma(k_q RN(omega/36), Y_q, f_q), one binary64
+//     FMA per population, Y_q = 36 (w_q T_q - F_q) / k_q an exact integer
+//     bracket (T_q = R + 3 c_q.J + C_q, the nonlinear terms C_q integer
+//     combinations of three double-float products); described at bgk_fma.
+//   shifted populations h = f - w (the plugin, bgk_fast<true>):
+//     C_q      = rho (4.5 (c_q.u)^2 - 1.5 u^2)           double-float, |C| <~ 1e-2
+//     T_q      = DH + 3 c_q.J + C_q                      integer (C_q's two
 //                                                        binary32 halves added exactly)
-//   f'_q     = fma(omega w_q, T_q, (1 - omega) f_q)      2 binary64 operations
-// which is f' = (1 - omega) f + omega feq with
-// feq_q = w_q (rho + 3 c.j + rho (4.5 (c.u)^2 - 1.5 u^2)), j = rho u.  The
-// rounded constants omega w_q are corrected for in fixed point (mass_k on the
-// rest population's R, mom_k on J in the 3 c.J terms) so that the zeroth and
-// first moments are relaxed with the factors omega sum w and
-// 3 omega sum c_x^2 w of the binary64 weights, as the reference relaxes them.
+//     h'_q     = fma(omega w_q, T_q, (1 - omega) h_q)    2 binary64 operations
+//   which is f' = (1 - omega) f + omega feq with
+//   feq_q = w_q (rho + 3 c.j + rho (4.5 (c.u)^2 - 1.5 u^2)), j = rho u.  The
+//   rounded constants omega w_q are corrected for in fixed point (mass_k on the
+//   rest population's DH, mom_k on J in the 3 c.J terms) so that the zeroth and
+//   first moments are relaxed with the factors omega sum w and
+//   3 omega sum c_x^2 w of the binary64 weights, as the reference relaxes them.
 //
 // TRT, incompressible (src/collision_trt.F90:98-152): for a pair p, m = -p
 // with v = c_p.J,
@@ -42,7 +47,8 @@
 // the double-float part formed from six merged Hermite coefficients (rr_fast).
 // TRT and RR use the lazy double-float operations (no renormalisation).
 //
-// Range.  The fast path takes |f_0| < 2, |f_axis| < 1/2, |f_diagonal| < 1/4
+// Range (TRT, RR and shifted BGK; bgk_fma states its own).  The fast path
+// takes |f_0| < 2, |f_axis| < 1/2, |f_diagonal| < 1/4
 // (biased binary64 exponent at most 1023, 1021, 1020).  Under these limits
 // every integer formed here stays below 16 * 2^59 < 2^63 in magnitude:
 // |R| < 5, |R + 3 c.J| < 11.5, |9 (F_p + F_m) - 2R| < 15,
@@ -382,6 +388,145 @@ DF_HD void bgk_fast(double (&f)[9], const Params& p, bool& bad) {
   PLBM_HY_PAIR(5, 7, df::add(ux, uy), JXc + JYc, 2)
   PLBM_HY_PAIR(8, 6, df::sub(ux, uy), JXc - JYc, 2)
 #undef PLBM_HY_PAIR
+}
+
+// ---- BGK with one binary64 FMA per population --------------------------------
+// f'_q = f_q + omega (feq_q - f_q), feq_q = w_q T_q, T_q = R + 3 c_q.J + C_q,
+// C_q = rho (4.5 (c_q.u)^2 - 1.5 u^2) (src/collision_bgk.F90:58-71 with the
+// equilibrium of src/fvm_bardow.F90:99-126, rearranged).  The nonlinear terms
+// of all nine populations are integer combinations of three products,
+//   A = 1.5 jx^2 / rho,  B = 1.5 jy^2 / rho,  X = 4.5 jx jy / rho,
+//   C_0 = -(A + B),  C_x = 2A - B,  C_y = 2B - A,  C_(+-diag) = 2 (A + B) +- 2X,
+// evaluated in double-float and taken to the fixed point once each.  With
+// every F_q and the C images integers, 36 (w_q T_q - F_q) is an integer, and
+//   rest      4 Y_0,  Y_0 = 4 (R + C_0) - 9 F_0
+//   axis      4 Y_q,  Y_q = T_q - 9 F_q
+//   diagonal    Y_q,  Y_q = T_q - 36 F_q
+// so f'_q = fma(k_q c, Y_q 2^-59, f_q) with c = RN(omega / 36), k_q = 4 or 1:
+// the only rounding of the linear part is the final one, and the integers
+// satisfy sum k_q Y_q = 0 and sum k_q c_q Y_q = 0 exactly (the nonlinear
+// combinations above sum to zero with the weights), so mass and momentum
+// change only by the nine final roundings.  Y_q is taken to binary64 by
+// integer instructions (53 leading bits); its error is relative to the small
+// non-equilibrium term, not to f.
+//
+// The reference relaxes with its binary64 weights, whose sum W0 + 4 WS + 4 WD
+// and first-moment factor 3 (2 WS + 4 WD) are both 1 - 2^-54: each step its
+// mass and momentum lose omega 2^-54 of themselves, 1e-12 over 10,000 steps
+// -- the size of the tolerance.  The same relaxation is restored in the
+// integers: the rest bracket gains omega eps_m R / (4c) (mass_k), and the
+// x-axis pair gains +- omega eps_j JX / (8c) (mom_k; the y pair likewise), so
+// the mass changes by omega eps_m R and JX by omega eps_j JX per step.
+//
+// Range.  The loads take 0 <= f_0 < 1, 0 <= f_axis < 1/4, 0 <= f_diag < 1/8
+// (biased exponents at most 1022, 1020, 1019), and the cell must satisfy
+// A + B < 0.2 (7.5 rho |u|^2 < 1, which bounds every |C_q| below 1).  Then,
+// in units of 2^59, R < 2.5, |JX|, |JY| < 1/2, |JX +- JY| < 3/4, and
+// |Y_0| < 10, |Y_axis| < 7.25, |Y_diag| < 10.25: every bracket fits int64
+// (intermediate products such as 4 R may wrap; two's complement sums of
+// wrapped terms are exact when the result fits).  Other cells report `bad`.
+struct BgkParams {
+  double c1;       // RN(omega / 36)
+  double c4;       // 4 RN(omega / 36), exact
+  int32_t mass_k;  // omega eps_m / c4 2^64, rounded (bgk_fma_params)
+  int32_t mom_k;   // omega eps_j / (2 c4) 2^64, rounded
+};
+
+// a + b = s + e exactly (Knuth's two-sum).
+inline void two_sum_d(double a, double b, double& s, double& e) {
+  s = a + b;
+  const double bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+// eps_m = W0 + 4 WS + 4 WD - 1 and eps_j = 3 (2 WS + 4 WD) - 1 of the binary64
+// weights, evaluated without rounding error (both are -2^-54 for 4/9, 1/9,
+// 1/36: the sums are within 2^-50 of 1, so the final subtraction is exact).
+inline double weight_sum_error(const double (&w)[3]) {
+  double s1, e1, s2, e2;
+  two_sum_d(w[0], 4.0 * w[1], s1, e1);
+  two_sum_d(s1, 4.0 * w[2], s2, e2);
+  return (s2 - 1.0) + (e1 + e2);
+}
+inline double first_moment_error(const double (&w)[3]) {
+  double s, e;
+  two_sum_d(2.0 * w[1], 4.0 * w[2], s, e);
+  const double p = 3.0 * s, ep = fma(3.0, s, -p);
+  return (p - 1.0) + (ep + 3.0 * e);
+}
+
+inline BgkParams bgk_fma_params(double omega, const double (&w)[3]) {
+  BgkParams p;
+  p.c1 = omega / 36.0;
+  p.c4 = 4.0 * p.c1;
+  const double eps_m = weight_sum_error(w), eps_j = first_moment_error(w);
+  const double km = ldexp(omega * eps_m / p.c4, 64), kj = ldexp(0.5 * omega * eps_j / p.c4, 64);
+  p.mass_k = fabs(km) < 0x1p30 ? (int32_t)llrint(km) : 0;
+  p.mom_k = fabs(kj) < 0x1p30 ? (int32_t)llrint(kj) : 0;
+  return p;
+}
+
+// Exact fixed-point image of a non-negative population below 2^(EMAX-1022);
+// `bad` for negative values, values past the limit and non-finite ones.
+PLBM_NOINLINE int64_t to_fixed_nonneg_slow(double d, int emax, int* bad) {
+  bool b = false;
+  const int64_t r = to_fixed_lim(d, emax, b);
+  if (b || r < 0) *bad = 1;
+  return r;
+}
+template <int EMAX>
+DF_HD int64_t to_fixed_nonneg(double d, bool& bad) {
+  const uint64_t u = df::d2u(d);
+  const uint32_t H = (uint32_t)(u >> 32), L = (uint32_t)u;
+  const uint32_t sh = (H >> 20) - 1016u;  // a set sign bit makes this large
+  if (sh <= (uint32_t)(EMAX - 1016)) {
+    const uint32_t mh = (H & 0xFFFFFu) | 0x100000u;
+    return (int64_t)(((uint64_t)funnel_l(L, mh, sh) << 32) | (uint64_t)(L << sh));
+  }
+  int b = 0;
+  const int64_t r = to_fixed_nonneg_slow(d, EMAX, &b);
+  if (b) bad = true;
+  return r;
+}
+
+DF_HD void bgk_fma(double (&f)[9], const BgkParams& p, bool& bad) {
+  using namespace df;
+  int64_t F[9];
+  F[0] = to_fixed_nonneg<1022>(f[0], bad);
+  F[1] = to_fixed_nonneg<1020>(f[1], bad);
+  F[2] = to_fixed_nonneg<1020>(f[2], bad);
+  F[3] = to_fixed_nonneg<1020>(f[3], bad);
+  F[4] = to_fixed_nonneg<1020>(f[4], bad);
+  F[5] = to_fixed_nonneg<1019>(f[5], bad);
+  F[6] = to_fixed_nonneg<1019>(f[6], bad);
+  F[7] = to_fixed_nonneg<1019>(f[7], bad);
+  F[8] = to_fixed_nonneg<1019>(f[8], bad);
+  const int64_t R = (((F[5] + F[7]) + (F[6] + F[8])) + ((F[1] + F[3]) + (F[2] + F[4]))) + F[0];
+  const int64_t d57 = F[5] - F[7], d86 = F[8] - F[6];
+  const int64_t JX = (d57 + d86) + (F[1] - F[3]);
+  const int64_t JY = (d57 - d86) + (F[2] - F[4]);
+  const df64 s15 = mul_f(recip(fixed_to_df(R)), 1.5f);  // 1.5 / rho
+  const df64 jx = fixed_to_df(JX), jy = fixed_to_df(JY);
+  const df64 A = mul_lz(sqr_lz(jx), s15);
+  const df64 B = mul_lz(sqr_lz(jy), s15);
+  const df64 X = mul_f_lz(mul_lz(mul_lz(jx, jy), s15), 3.0f);
+  bad |= !(A.hi + B.hi < 0.2f);  // NaN (R = 0) fails too
+  const int64_t Ai = df_to_fixed(A), Bi = df_to_fixed(B), Xi = df_to_fixed(X);
+  const int64_t AB = Ai + Bi;
+  f[0] = fma_d(p.c4, fixed_to_double_any(4 * (R - AB) - 9 * F[0] + scale_2m64(R, p.mass_k)), f[0]);
+  const int64_t cx = R + (2 * Ai - Bi), cy = R + (2 * Bi - Ai);
+  const int64_t jx3 = 3 * JX, jy3 = 3 * JY;
+  const int64_t ax = jx3 + scale_2m64(JX, p.mom_k), ay = jy3 + scale_2m64(JY, p.mom_k);
+  f[1] = fma_d(p.c4, fixed_to_double_any(cx + ax - 9 * F[1]), f[1]);
+  f[3] = fma_d(p.c4, fixed_to_double_any(cx - ax - 9 * F[3]), f[3]);
+  f[2] = fma_d(p.c4, fixed_to_double_any(cy + ay - 9 * F[2]), f[2]);
+  f[4] = fma_d(p.c4, fixed_to_double_any(cy - ay - 9 * F[4]), f[4]);
+  const int64_t dp = R + 2 * (AB + Xi), dm = R + 2 * (AB - Xi);
+  const int64_t sp = jx3 + jy3, sm = jy3 - jx3;
+  f[5] = fma_d(p.c1, fixed_to_double_any(dp + sp - 36 * F[5]), f[5]);
+  f[7] = fma_d(p.c1, fixed_to_double_any(dp - sp - 36 * F[7]), f[7]);
+  f[6] = fma_d(p.c1, fixed_to_double_any(dm + sm - 36 * F[6]), f[6]);
+  f[8] = fma_d(p.c1, fixed_to_double_any(dm - sm - 36 * F[8]), f[8]);
 }
 
 // Incompressible TRT constants (index 0: axis pairs, 1: diagonal pairs).

@@ -12,7 +12,7 @@ constexpr int kBatchMaxThreads = 512;
 // One grid of a batch, as the kernels see it.
 struct alignas(16) BatchGrid {
   CollParams p;       // relaxation parameters (grid's omega / TRT magic)
-  hy::Params hp;      // the same for the hybrid binary64 BGK
+  hy::BgkParams hp;   // the same for the hybrid binary64 BGK (bgk_fma)
   hy::TrtParams ht;   // ... and TRT
   long long off;      // element offset of lattice A; lattice B follows it
   int nx, ny, ld;
@@ -23,7 +23,7 @@ struct alignas(16) BatchGrid {
   int pad;
 };
 
-hy::Params hybrid_params(double omega);
+hy::BgkParams hybrid_bgk_params(double omega);
 hy::TrtParams hybrid_trt_params(const CollParams& p);
 
 struct BatchLaunch {

@@ -96,7 +96,8 @@ df::df64 split_const(double d) {
 // Constants of one hybrid launch: the hybrid operator's and the binary64
 // operator's (for cells outside the hybrid range).
 struct HybridArgs {
-  hy::Params bgk;
+  hy::BgkParams bgk1;  // BGK on populations (bgk_fma)
+  hy::Params bgk;      // BGK on shifted populations (the plugin, bgk_fast<true>)
   hy::TrtParams trt;
   hy::RrParams rr;
   CollParams ref;
@@ -120,10 +121,11 @@ __device__ __noinline__ void hybrid_fallback_cell(const double* __restrict__ src
   g_hybrid_range_flag = 1;
 }
 
-// Resident CTAs per SM the hybrid kernels are compiled for (register cap
-// 65536 / (256 x this) = 48 registers): measured best at 8192^2 for BGK, TRT
-// and RR alike (4 CTAs: TRT 1 % slower; 6: BGK 2 %, RR 4 % slower).
-constexpr int hybrid_min_blocks(int) { return 5; }
+// Resident CTAs per SM the hybrid kernels are compiled for: TRT and RR at 5
+// (register cap 65536 / (256 x 5) = 48; measured best at 8192^2: 4 CTAs made
+// TRT 1 % slower, 6 made RR 4 % slower); BGK (bgk_fma) at 4, 64 registers,
+// which it needs without spills.
+constexpr int hybrid_min_blocks(int kind) { return kind == K_BGK ? 4 : 5; }
 
 // I: index type of the lattice offsets; 32-bit when the whole lattice has
 // fewer than 2^32 elements (one multiply-add per address instead of 64-bit
@@ -151,7 +153,7 @@ __global__ void __launch_bounds__(kBlock, hybrid_min_blocks(KIND)) k_step_hybrid
   bool bad = false;
   if (KIND == K_TRT) hy::trt_fast(f, a.trt, bad);
   else if (KIND == K_RR) hy::rr_fast(f, a.rr, bad);
-  else hy::bgk_fast(f, a.bgk, bad);
+  else hy::bgk_fma(f, a.bgk1, bad);
   if (bad) {  // outside the hybrid range: the binary64 operator on the same inputs
     hybrid_fallback_cell<KIND>(src, dst, x, y, nx, ny, ld, a.ref);
     return;
@@ -188,7 +190,7 @@ __global__ void __launch_bounds__(kBlock) k_step_scheme_hybrid(const double* __r
   bool bad = false;
   if (KIND == K_TRT) hy::trt_fast(f, a.trt, bad);
   else if (KIND == K_RR) hy::rr_fast(f, a.rr, bad);
-  else hy::bgk_fast(f, a.bgk, bad);
+  else hy::bgk_fma(f, a.bgk1, bad);
   if (bad) {
     scheme_fallback_cell<TAPS, KIND>(src, dst, x, y, nx, ny, ld, st, a.ref);
     return;
@@ -261,6 +263,11 @@ cudaError_t launch_hybrid(const Sweep& s, unsigned blocks, int bs, int ft, const
 
 }  // namespace
 
+hy::BgkParams hybrid_bgk_params(double omega) {
+  const double w[3] = {W0, WS, WD};
+  return hy::bgk_fma_params(omega, w);
+}
+
 hy::Params hybrid_params(double omega) {
   hy::Params p;
   p.omb = 1.0 - omega;
@@ -309,6 +316,7 @@ cudaError_t step_pull_df64(int kind, const Sweep& s, const CollParams& cp) {
   const long long blocks = (long long)ft * s.nx;
   if (blocks <= 0 || blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
   HybridArgs a;
+  a.bgk1 = hybrid_bgk_params(cp.omega);
   a.bgk = hybrid_params(cp.omega);
   a.trt = hybrid_trt_params(cp);
   a.rr = hybrid_rr_params(cp);
@@ -325,6 +333,7 @@ cudaError_t step_push_hybrid(int kind, const Sweep& s, const CollParams& cp) {
   const long long blocks = (long long)ft * s.ny;
   if (blocks <= 0 || blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
   HybridArgs a;
+  a.bgk1 = hybrid_bgk_params(cp.omega);
   a.bgk = hybrid_params(cp.omega);
   a.trt = hybrid_trt_params(cp);
   a.rr = hybrid_rr_params(cp);
@@ -356,6 +365,7 @@ cudaError_t step_scheme_hybrid(int scheme, int kind, const Sweep& s, double dt, 
   if (blocks <= 0 || blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
   const sch::Stencil st = sch::stencil_coefficients(scheme, dt);
   HybridArgs a;
+  a.bgk1 = hybrid_bgk_params(cp.omega);
   a.bgk = hybrid_params(cp.omega);
   a.trt = hybrid_trt_params(cp);
   a.rr = hybrid_rr_params(cp);
