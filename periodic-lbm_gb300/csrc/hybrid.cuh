@@ -390,6 +390,102 @@ DF_HD void bgk_fast(double (&f)[9], const Params& p, bool& bad) {
 #undef PLBM_HY_PAIR
 }
 
+// ---- conversions shaped for the GB300 pipes ----------------------------------
+// Measured issue rates per SM and clock: integer add/logic/shift and
+// I2F.F32.S32 go to the ALU pipe (64 lanes), IMAD and binary32 arithmetic to
+// the FMA pipes (64 / 128), F2I, FRND and FLO (clz) to the XU pipe (16), and
+// every conversion to or from a 64-bit type to the binary64 pipe (~2).  The
+// one-FMA BGK is bound by its ALU work, so these forms move work to the FMA
+// and XU pipes.
+
+// 32-bit count of leading zeros (XU pipe).
+DF_HD uint32_t clz32(uint32_t a) {
+#ifdef __CUDA_ARCH__
+  return (uint32_t)__clz((int)a);
+#else
+  return a ? (uint32_t)__builtin_clz(a) : 32u;
+#endif
+}
+// Low word of (hi:lo) >> sh, 0 <= sh <= 31.
+DF_HD uint32_t funnel_r(uint32_t lo, uint32_t hi, uint32_t sh) {
+#ifdef __CUDA_ARCH__
+  return __funnelshift_r(lo, hi, sh);
+#else
+  return sh ? (lo >> sh) | (hi << (32 - sh)) : lo;
+#endif
+}
+DF_HD int32_t f2i_trunc(float v) {
+#ifdef __CUDA_ARCH__
+  return __float2int_rz(v);
+#else
+  return (int32_t)v;
+#endif
+}
+DF_HD float i2f(int32_t v) {
+#ifdef __CUDA_ARCH__
+  return __int2float_rn(v);
+#else
+  return (float)v;
+#endif
+}
+
+PLBM_NOINLINE double fixed_to_double_any_slow(int64_t T) { return fixed_to_double_any(T); }
+
+// int64 fixed point (scale 2^59) -> binary64 for |T| >= 2^32 (others out of
+// line, exactly): the magnitude taken in one's complement (a negative T comes
+// out 2^-59 smaller in magnitude) and truncated to 53 bits.  The error is below
+// 2^-52 relative plus 2^-59 absolute -- for the non-equilibrium brackets it
+// converts, negligible against the binary64 rounding of the populations.
+DF_HD double fixed_to_double_tr(int64_t T) {
+  const uint32_t hi = (uint32_t)((uint64_t)T >> 32), lo = (uint32_t)(uint64_t)T;
+  const uint32_t s = (uint32_t)((int32_t)hi >> 31);  // 0 or ~0
+  const uint32_t ah = hi ^ s, al = lo ^ s;
+  if (ah == 0u) return fixed_to_double_any_slow(T);
+  const uint32_t lz = clz32(ah);  // 0..31
+  const uint32_t nh = funnel_l(al, ah, lz), nl = al << lz;  // bit 63 of (nh:nl) set
+  const uint32_t mh = nh >> 11, ml = funnel_r(nl, nh, 11);  // 53 bits, leading one at bit 52
+  // value = (nh:nl) 2^(-lz - 59): biased exponent 1027 - lz; the leading one of
+  // mh (bit 20) adds the final 1 to the exponent field
+  const uint32_t eh = (1026u - lz) * 0x100000u + mh;
+  return df::u2d(((uint64_t)(eh | (s & 0x80000000u)) << 32) | (uint64_t)ml);
+}
+
+// binary32 v, |v| < 16 -> int64 fixed point (scale 2^59), truncated toward
+// zero below 2^-58: the integer part of v 2^27 (F2I) is the high word and its
+// fraction 2^31 (F2I, signed) the low word shifted by one.  The fraction
+// t - trunc(t) is exact for either sign.  Exact for |v| >= 2^-35.
+DF_HD int64_t float_to_fixed_xu(float v) {
+  const float t = v * 0x1p27f;  // exact
+  const int32_t h = f2i_trunc(t);
+  const int32_t l = f2i_trunc((t - i2f(h)) * 0x1p31f);  // |l| < 2^31
+  return (int64_t)((uint64_t)(uint32_t)h << 32) + 2 * (int64_t)l;
+}
+// A double-float (|value| < 16) in the fixed point: the sum of its halves' images.
+DF_HD int64_t df_to_fixed_xu(df64 c) { return float_to_fixed_xu(c.hi) + float_to_fixed_xu(c.lo); }
+
+PLBM_NOINLINE df64 fixed_to_df_slow(int64_t T) { return fixed_to_df(T); }
+
+// int64 fixed point -> double-float (leading 48 bits: hi and lo truncated)
+// for |T| >= 2^32 (others out of line).
+DF_HD df64 fixed_to_df_x(int64_t T) {
+  const uint32_t hi = (uint32_t)((uint64_t)T >> 32), lo = (uint32_t)(uint64_t)T;
+  const uint32_t s = (uint32_t)((int32_t)hi >> 31);
+  const uint64_t a = ((((uint64_t)hi << 32) | lo) ^ (((uint64_t)s << 32) | s)) + (uint64_t)(s & 1u);
+  const uint32_t ah = (uint32_t)(a >> 32), al = (uint32_t)a;
+  if (ah == 0u) return fixed_to_df_slow(T);
+  const uint32_t lz = clz32(ah);
+  const uint32_t nh = funnel_l(al, ah, lz), nl = al << lz;  // bit 31 of nh set
+  // value = (nh:nl) 2^(-lz - 59) = nh 2^(-lz - 27) + ...: hi = top 24 bits of
+  // nh, leading one at bit 23 (it adds the final 1 to the exponent field)
+  const uint32_t sgn = s & 0x80000000u;
+  const float fhi = df::u2f_bits(((130u - lz) * 0x800000u + (nh >> 8)) | sgn);
+  const uint32_t ml = funnel_r(nl, nh, 16) & 0xFFFFFFu;  // next 24 bits
+  // lo = ml 2^(16 - lz - 59): a signed scale (biased exponent 84 - lz) times
+  // the exact I2F of the 24-bit integer
+  const float sc = df::u2f_bits(((84u - lz) * 0x800000u) | sgn);
+  return df::make(fhi, i2f((int32_t)ml) * sc);
+}
+
 // ---- BGK with one binary64 FMA per population --------------------------------
 // f'_q = f_q + omega (feq_q - f_q), feq_q = w_q T_q, T_q = R + 3 c_q.J + C_q,
 // C_q = rho (4.5 (c_q.u)^2 - 1.5 u^2) (src/collision_bgk.F90:58-71 with the
@@ -505,28 +601,28 @@ DF_HD void bgk_fma(double (&f)[9], const BgkParams& p, bool& bad) {
   const int64_t d57 = F[5] - F[7], d86 = F[8] - F[6];
   const int64_t JX = (d57 + d86) + (F[1] - F[3]);
   const int64_t JY = (d57 - d86) + (F[2] - F[4]);
-  const df64 s15 = mul_f(recip(fixed_to_df(R)), 1.5f);  // 1.5 / rho
-  const df64 jx = fixed_to_df(JX), jy = fixed_to_df(JY);
+  const df64 s15 = mul_f(recip(fixed_to_df_x(R)), 1.5f);  // 1.5 / rho
+  const df64 jx = fixed_to_df_x(JX), jy = fixed_to_df_x(JY);
   const df64 A = mul_lz(sqr_lz(jx), s15);
   const df64 B = mul_lz(sqr_lz(jy), s15);
   const df64 X = mul_f_lz(mul_lz(mul_lz(jx, jy), s15), 3.0f);
   bad |= !(A.hi + B.hi < 0.2f);  // NaN (R = 0) fails too
-  const int64_t Ai = df_to_fixed(A), Bi = df_to_fixed(B), Xi = df_to_fixed(X);
+  const int64_t Ai = df_to_fixed_xu(A), Bi = df_to_fixed_xu(B), Xi = df_to_fixed_xu(X);
   const int64_t AB = Ai + Bi;
-  f[0] = fma_d(p.c4, fixed_to_double_any(4 * (R - AB) - 9 * F[0] + scale_2m64(R, p.mass_k)), f[0]);
+  f[0] = fma_d(p.c4, fixed_to_double_tr(4 * (R - AB) - 9 * F[0] + scale_2m64(R, p.mass_k)), f[0]);
   const int64_t cx = R + (2 * Ai - Bi), cy = R + (2 * Bi - Ai);
   const int64_t jx3 = 3 * JX, jy3 = 3 * JY;
   const int64_t ax = jx3 + scale_2m64(JX, p.mom_k), ay = jy3 + scale_2m64(JY, p.mom_k);
-  f[1] = fma_d(p.c4, fixed_to_double_any(cx + ax - 9 * F[1]), f[1]);
-  f[3] = fma_d(p.c4, fixed_to_double_any(cx - ax - 9 * F[3]), f[3]);
-  f[2] = fma_d(p.c4, fixed_to_double_any(cy + ay - 9 * F[2]), f[2]);
-  f[4] = fma_d(p.c4, fixed_to_double_any(cy - ay - 9 * F[4]), f[4]);
+  f[1] = fma_d(p.c4, fixed_to_double_tr(cx + ax - 9 * F[1]), f[1]);
+  f[3] = fma_d(p.c4, fixed_to_double_tr(cx - ax - 9 * F[3]), f[3]);
+  f[2] = fma_d(p.c4, fixed_to_double_tr(cy + ay - 9 * F[2]), f[2]);
+  f[4] = fma_d(p.c4, fixed_to_double_tr(cy - ay - 9 * F[4]), f[4]);
   const int64_t dp = R + 2 * (AB + Xi), dm = R + 2 * (AB - Xi);
   const int64_t sp = jx3 + jy3, sm = jy3 - jx3;
-  f[5] = fma_d(p.c1, fixed_to_double_any(dp + sp - 36 * F[5]), f[5]);
-  f[7] = fma_d(p.c1, fixed_to_double_any(dp - sp - 36 * F[7]), f[7]);
-  f[6] = fma_d(p.c1, fixed_to_double_any(dm + sm - 36 * F[6]), f[6]);
-  f[8] = fma_d(p.c1, fixed_to_double_any(dm - sm - 36 * F[8]), f[8]);
+  f[5] = fma_d(p.c1, fixed_to_double_tr(dp + sp - 36 * F[5]), f[5]);
+  f[7] = fma_d(p.c1, fixed_to_double_tr(dp - sp - 36 * F[7]), f[7]);
+  f[6] = fma_d(p.c1, fixed_to_double_tr(dm + sm - 36 * F[6]), f[6]);
+  f[8] = fma_d(p.c1, fixed_to_double_tr(dm - sm - 36 * F[8]), f[8]);
 }
 
 // Incompressible TRT constants (index 0: axis pairs, 1: diagonal pairs).
