@@ -2,7 +2,7 @@
  * plbm_plugin.h -- the reference's simulation-plugin C ABI, served by
  * libplbmgpu.so under the stem "plbmgpu".
  *
- * Replaces the Fortran plugin sim/sim_slbm.F90:155-228 (prototypes in
+ * Replaces the Fortran plugin sim/sim_slbm.F90:135-205 (prototypes in
  * sim/lbm.h:13-19).  A loader derives the symbol names from the library file
  * stem (sim/cases.py:21-32): libplbmgpu.so -> c_plbmgpu_{init,step,vars,free,norm}.
  *
@@ -13,7 +13,7 @@
  *  - populations are stored shifted, h_i = f_i - w_i (sim/sim.F90:131,384);
  *  - a step is collide-then-push-stream with periodic wrap
  *    (sim/sim.F90:404-505 + :568-624);
- *  - dt must be 1.0 (sim/sim_slbm.F90:71-74).
+ *  - dt must be 1.0 (sim/sim_slbm.F90:48-51).
  * Where the reference stops the program (error stop), these entry points
  * return NULL / set a sticky error instead; read it with plbm_last_error()
  * and c_plbmgpu_status().
@@ -37,16 +37,16 @@ typedef struct plbm_plugin_params {
                           arithmetic on the shifted populations)           */
 } plbm_plugin_params;
 
-/* siminit -- sim/lbm.h:13-15, sim/sim_slbm.F90:158-172 */
+/* siminit -- sim/lbm.h:13-15, c_slbm_init sim/sim_slbm.F90:135-149 (slbm_init :41-78) */
 void *c_plbmgpu_init(int nx, int ny, double dt, const double *rho, const double *u,
                      const double *sigma, void *params);
-/* simstep -- sim/lbm.h:17, sim/sim_slbm.F90:175-183 */
+/* simstep -- sim/lbm.h:17, c_slbm_step sim/sim_slbm.F90:152-160 (slbm_step :80-110) */
 void c_plbmgpu_step(void *sim, double omega);
-/* simvars -- sim/lbm.h:18, sim/sim_slbm.F90:186-203 */
+/* simvars -- sim/lbm.h:18, c_slbm_vars sim/sim_slbm.F90:163-180 (slbm_vars :112-127) */
 void c_plbmgpu_vars(void *sim, double *rho, double *u);
-/* simfree -- sim/lbm.h:19, sim/sim_slbm.F90:207-218 */
+/* simfree -- sim/lbm.h:19, c_slbm_free sim/sim_slbm.F90:184-195 */
 void c_plbmgpu_free(void *sim);
-/* norm2(u-ua)/norm2(ua) -- sim/sim_slbm.F90:221-228 (host arithmetic) */
+/* norm2(u-ua)/norm2(ua) -- c_slbm_norm sim/sim_slbm.F90:198-205 (host arithmetic) */
 double c_plbmgpu_norm(int nx, int ny, const double *u, const double *ua);
 /* Not in the reference: sticky status of a plugin instance (0 = ok). */
 int c_plbmgpu_status(void *sim);

@@ -265,7 +265,7 @@ def sim_macros(f: np.ndarray):
 
 
 def sim_slbm_steps(f1: np.ndarray, omega: float, nsteps: int) -> np.ndarray:
-    """nsteps plugin steps starting from f1 (f2 = f1 initially, sim/sim_slbm.F90:99)."""
+    """nsteps plugin steps starting from f1 (f2 = f1 initially, sim/sim_slbm.F90:76)."""
     ny, nx = f1.shape[1] - 2, f1.shape[2] - 2
     a = f1.copy()
     b = f1.copy()

@@ -889,7 +889,7 @@ void oref_sim_bc_push(int nx, int ny, double *f)
     f[HIDX(1, 1, 5)] = f[HIDX(nx + 1, ny + 1, 5)];
 }
 
-/* sim/sim_slbm.F90:103-133 (gfortran branch: collide+push, bc, move_alloc swap).
+/* sim/sim_slbm.F90:80-110 (gfortran branch: collide+push, bc, move_alloc swap).
  * On return f1 holds the current state, as after the reference's swap. */
 void oref_sim_slbm_steps(int nx, int ny, double *f1, double *f2, double omega, int nsteps)
 {
@@ -910,7 +910,7 @@ void oref_sim_slbm_steps(int nx, int ny, double *f1, double *f2, double omega, i
     }
 }
 
-/* sim/sim_slbm.F90:221-228: norm2(u - ua) / norm2(ua) */
+/* sim/sim_slbm.F90:198-205: norm2(u - ua) / norm2(ua) */
 double oref_sim_norm(int nx, int ny, const double *u, const double *ua)
 {
     double a = 0.0, b = 0.0;

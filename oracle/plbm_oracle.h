@@ -88,9 +88,9 @@ void oref_sim_macros(int nx, int ny, int nhalo, const double *f, double *rho, do
 void oref_sim_collide_stream_fused(int nx, int ny, const double *fsrc, double *fdst, double omega);
 /* sim/sim.F90:568-624 */
 void oref_sim_bc_push(int nx, int ny, double *f);
-/* sim/sim_slbm.F90:103-133, nsteps steps with the move_alloc swap (f1 <-> f2 pointers) */
+/* sim/sim_slbm.F90:80-110, nsteps steps with the move_alloc swap (f1 <-> f2 pointers) */
 void oref_sim_slbm_steps(int nx, int ny, double *f1, double *f2, double omega, int nsteps);
-/* sim/sim_slbm.F90:221-228 */
+/* sim/sim_slbm.F90:198-205 */
 double oref_sim_norm(int nx, int ny, const double *u, const double *ua);
 
 /* ---- discrete adjoint of the BGK time stepper (no reference counterpart) --

@@ -129,7 +129,7 @@ int do_steps(PluginSim* s, double omega, int nsteps) {
   for (int i = 0; i < nsteps; i++) {
     cudaError_t e = push_step(s, s->cur, p);
     if (e != cudaSuccess) return s->status = cuda_fail(e, "plugin step kernel");
-    s->cur = 1 - s->cur;  // move_alloc swap, sim/sim_slbm.F90:114-119
+    s->cur = 1 - s->cur;  // move_alloc swap, sim/sim_slbm.F90:91-95
   }
   return PLBM_OK;
 }
@@ -142,11 +142,11 @@ extern "C" void* c_plbmgpu_init(int nx, int ny, double dt, const double* rho, co
     fail(PLBM_E_INVALID, "grid size %dx%d", nx, ny);
     return nullptr;
   }
-  if (dt != 1.0) {  // sim/sim_slbm.F90:71-74
+  if (dt != 1.0) {  // sim/sim_slbm.F90:48-51
     fail(PLBM_E_INVALID, "Standard LBM only supports dt = 1.0 (got %g)", dt);
     return nullptr;
   }
-  if (sigma) {  // sim/sim_slbm.F90:88-93
+  if (sigma) {  // sim/sim_slbm.F90:64-70
     fail(PLBM_E_UNSUPPORTED, "non-equilibrium initialisation (sigma) is not implemented");
     return nullptr;
   }
@@ -214,7 +214,7 @@ extern "C" void* c_plbmgpu_init(int nx, int ny, double dt, const double* rho, co
   if (e == cudaSuccess)
     e = equilibrium(st_code(storage), 1, nx, ny, s->ld, s->scratch, s->scratch + n, s->scratch + 2 * n, 1, s->f[0],
                     s->stream);
-  // this%grid%f2 = this%grid%f1, sim/sim_slbm.F90:99
+  // this%grid%f2 = this%grid%f1, sim/sim_slbm.F90:76
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(s->f[1], s->f[0], s->lat_elems * s->elem_bytes, cudaMemcpyDeviceToDevice, s->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
@@ -256,7 +256,7 @@ extern "C" void c_plbmgpu_vars(void* p, double* rho, double* u) {
   }
   const size_t n = (size_t)s->nx * s->ny;
   cudaError_t e = cudaSetDevice(s->device);
-  // lbm_macros of the current state, sim/sim_slbm.F90:135-150
+  // lbm_macros of the current state, sim/sim_slbm.F90:112-127
   if (e == cudaSuccess)
     e = macros(st_code(s->storage), 1, s->nx, s->ny, s->ld, s->f[s->cur], s->scratch, s->scratch + n,
                s->scratch + 2 * n, s->stream);
@@ -288,7 +288,7 @@ extern "C" int c_plbmgpu_status(void* p) {
 }
 
 extern "C" double c_plbmgpu_norm(int nx, int ny, const double* u, const double* ua) {
-  // norm2(u - ua) / norm2(ua), sim/sim_slbm.F90:221-228
+  // norm2(u - ua) / norm2(ua), sim/sim_slbm.F90:198-205
   if (nx < 1 || ny < 1 || !u || !ua) return NAN;
   double a = 0.0, b = 0.0;
   const size_t n = (size_t)nx * ny;

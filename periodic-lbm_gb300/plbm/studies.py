@@ -130,7 +130,7 @@ def tgv_case(n: int, base: int, dt_over_tau: float | None, re: float = 1.0):
     """Parameters of one refinement level of sim/cases.py:main (:252-282).
 
     dt_over_tau=None takes dt = 1 (lattice units), which the lattice Boltzmann
-    plugins require (sim/sim_slbm.F90:71-74); the reference's study sets
+    plugins require (sim/sim_slbm.F90:48-51); the reference's study sets
     dt = (dt/tau) tau for its finite-difference plugins."""
     umax = 0.01 / (n / base)
     k = (2 * math.pi / n, 2 * math.pi / n)

@@ -106,10 +106,10 @@ def test_plugin_init_rejects_reference_error_cases(lib):
     nx, ny = 4, 3
     p = np.zeros((nx, ny), order="F")
     u = np.zeros((nx, ny, 2), order="F")
-    # dt /= 1 (sim/sim_slbm.F90:71-74)
+    # dt /= 1 (sim/sim_slbm.F90:48-51)
     assert not lib.c_plbmgpu_init(nx, ny, 0.5, p.ctypes.data, u.ctypes.data, None, None)
     assert "dt = 1.0" in _lib.last_error()
-    # sigma present (sim/sim_slbm.F90:88-93)
+    # sigma present (sim/sim_slbm.F90:64-70)
     s = np.zeros((nx, ny, 3), order="F")
     assert not lib.c_plbmgpu_init(nx, ny, 1.0, p.ctypes.data, u.ctypes.data, s.ctypes.data, None)
     assert "sigma" in _lib.last_error()

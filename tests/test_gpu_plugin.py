@@ -235,3 +235,44 @@ def test_plugin_hybrid_needs_f64(gpu_lib):
     sim = SimPlugin()
     with pytest.raises(PlbmError):
         sim.init((16, 16), 1.0, p, u, params=make_params(storage="f32dev", math="hybrid"))
+
+
+REFERENCE_FIXTURE = __import__("pathlib").Path(__file__).resolve().parent / "golden" / "reference_plugin.npz"
+
+
+@pytest.mark.parametrize("case", ["n10", "n20", "n40", "rect48x32"])
+@pytest.mark.parametrize("math_mode,tol", [("strict", 0.0), ("fma", 1e-12), ("hybrid", 1e-12)])
+def test_reference_study_fixture(gpu_lib, case, math_mode, tol):
+    """libplbmgpu.so, started from the fields the reference's TGVStudy built
+    and run the reference study's step count, against the state the
+    reference's own SimPlugin and run produced over the oracle plugin
+    (tests/golden/reference_plugin.npz, made by make_reference_fixtures.py):
+    strict bit-identical, FMA and hybrid within 1e-12; the study's error norms
+    recomputed here (plbm.studies.TGVStudy, the plugin's norm) equal the
+    reference's to 1e-9 (the analytic solution is re-evaluated on this
+    machine, whose numpy sin/cos/exp may differ from the fixture machine's in
+    the last ulp)."""
+    from plbm.plugin import SimPlugin, make_params
+    from plbm.studies import TGVStudy, run
+    z = np.load(REFERENCE_FIXTURE)
+    umax, kx, ky, nu, omega, nsteps, tend = z[case + "_params"]
+    p0, u0 = z[case + "_p0"], z[case + "_u0"]
+    grid_size = p0.shape
+    sim = SimPlugin()
+    sim.init(grid_size, 1.0, p0, u0, params=make_params(math=math_mode))
+    tm, _ = run(sim, omega, int(nsteps))
+    rho, u = sim.vars()
+    study = TGVStudy(grid_size, umax=umax, k=(kx, ky), nu=nu)
+    _, uref = study.solution(t=tm)
+    norms = np.array([study.norm1(tm, u), study.norm2(tm, u), sim.my_norm(u[:, :, 0], uref[:, :, 0]),
+                      study.norm2x(tm, u[:, :, 0]), study.norm2y(tm, u[:, :, 1])])
+    sim.free()
+    assert tm == tend
+    r_ref, u_ref = z[case + "_rho"], z[case + "_u"]
+    rel = lambda a, b: float(np.max(np.abs(a - b)) / np.max(np.abs(b)))  # noqa: E731
+    errs = (rel(rho, r_ref), rel(u[:, :, 0], u_ref[:, :, 0]), rel(u[:, :, 1], u_ref[:, :, 1]))
+    if tol == 0.0:
+        assert np.array_equal(rho, r_ref) and np.array_equal(u, u_ref), errs
+    else:
+        assert max(errs) <= tol, errs
+    np.testing.assert_allclose(norms, z[case + "_norms"], rtol=1e-9)
