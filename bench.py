@@ -6,9 +6,9 @@ Headline workload: plain single-grid bandwidth bench, D2Q9 BGK, tau = 0.6,
 Taylor-Green vortex u0 = 0.05 (k = 2 pi / 8192) plus seeded i.i.d.
 N(0, 1e-4^2) velocity noise, f at equilibrium.  A step is one
 perform_lbm_step (one fused pull-stream + collide kernel) over the grid.
-The headline arithmetic is PLBM_MATH_HYBRID (binary64 storage and final
-FMAs, exact integer moments; see DESIGN notes in the package); the straight
-binary64 kernel is measured beside it ("variants.fp64_native").
+The headline arithmetic is PLBM_MATH_HYBRID (binary64 storage, one binary64
+FMA per population on an exact integer bracket, exact integer moments); the
+straight binary64 kernel is measured beside it ("variants.fp64_native").
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                     [--n 8192] [--kind bgk|trt|rr] [--storage f64|f32dev|f16dev]

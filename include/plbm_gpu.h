@@ -196,15 +196,18 @@ int plbm_velocity_l2_error(plbm_grid_t *g, int ibuf, const double *uxa, const do
  * f is a DEVICE lattice f(ld,nx,0:8) of the given storage; uxa, uya are host
  * (ny,nx) fields; err is a host double.  Nothing is allocated: the reference
  * fields and the partial sums are staged in one fixed device array of
- * 2*PLBM_NOALLOC_MAX_CELLS + 3648 doubles (about 16 MB), reserved on every GPU
- * that loads the library until exit.  nx*ny > PLBM_NOALLOC_MAX_CELLS returns
- * PLBM_E_INVALID.  The first call on a device looks up the array's device
+ * 2*PLBM_NOALLOC_MAX_CELLS + PLBM_NOALLOC_PARTIAL_DOUBLES doubles (about 16 MB),
+ * reserved on every GPU that loads the library until exit.
+ * nx*ny > PLBM_NOALLOC_MAX_CELLS returns PLBM_E_INVALID, and so do extents
+ * above PLBM_MAX_EXTENT.  The first call on a device looks up the array's device
  * address (cudaGetSymbolAddress) with that device current; make that first
  * call before any stream capture.  All calls share the array and it keeps the
  * last call's contents, so calls that overlap on the GPU (other streams,
- * other host threads) race; serialise them.  Runs on cuda_stream (may be
+ * other host threads) race; serialise them: the library's lock covers only
+ * the first call's address lookup, not the calls.  Runs on cuda_stream (may be
  * NULL) and returns after the result is on the host. */
 #define PLBM_NOALLOC_MAX_CELLS (1 << 20)
+#define PLBM_NOALLOC_PARTIAL_DOUBLES 3648
 int plbm_velocity_l2_error_noalloc(int storage, int nx, int ny, int ld, const void *f,
                                    const double *uxa, const double *uya, double *err,
                                    void *cuda_stream);

@@ -173,7 +173,6 @@ __global__ void __launch_bounds__(kBlock) k_vorticity(const double* __restrict__
 #undef A
 }
 
-constexpr int kReduceBlocks = 1216;  // 152 SMs x 8
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll

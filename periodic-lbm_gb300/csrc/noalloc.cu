@@ -12,8 +12,8 @@
 //
 // The staging array (g_noalloc_scratch below) holds the two reference fields
 // of at most PLBM_NOALLOC_MAX_CELLS cells plus the per-block partial sums:
-// 2 * 2^20 + 3 * 1216 doubles, about 16 MB, reserved on every GPU that loads
-// the library until the process exits.
+// 2 * 2^20 + 3 * kReduceBlocks doubles, about 16 MB, reserved on every GPU that
+// loads the library until the process exits.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <mutex>
@@ -31,8 +31,10 @@ using plbm_internal::fail;
 namespace {
 
 constexpr size_t kMaxCells = (size_t)1 << 20;  // PLBM_NOALLOC_MAX_CELLS
-constexpr int kMaxPartials = 1216;             // reduction blocks (152 SMs x 8)
+constexpr int kMaxPartials = plbm::kReduceBlocks;  // one partial triple per reduction block
 constexpr size_t kScratchDoubles = 2 * kMaxCells + 3 * (size_t)kMaxPartials;
+static_assert(kMaxCells == (size_t)PLBM_NOALLOC_MAX_CELLS, "staging capacity");
+static_assert(3 * kMaxPartials == PLBM_NOALLOC_PARTIAL_DOUBLES, "partial-sum staging, as the header states it");
 
 // Shared by every call on a device; keeps the last call's contents.
 static __device__ __align__(256) double g_noalloc_scratch[kScratchDoubles];
@@ -43,7 +45,8 @@ double* g_addr[kMaxDevices] = {};
 
 // Device address of g_noalloc_scratch for the current device, looked up once
 // per device with that device current.  In host code the symbol's name is a
-// host-side stand-in, never a device address.
+// host-side stand-in, never a device address.  The mutex guards this lookup
+// only; it does not serialise the calls that use the array.
 int scratch_address(double** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -65,7 +68,8 @@ int scratch_address(double** out) {
 extern "C" int plbm_velocity_l2_error_noalloc(int storage, int nx, int ny, int ld, const void* f,
                                               const double* uxa, const double* uya, double* err,
                                               void* cuda_stream) {
-  if (nx < 1 || ny < 1 || ld < ny) return fail(PLBM_E_INVALID, "bad sizes nx=%d ny=%d ld=%d", nx, ny, ld);
+  if (nx < 1 || ny < 1 || ld < ny || nx > PLBM_MAX_EXTENT || ld > PLBM_MAX_EXTENT)
+    return fail(PLBM_E_INVALID, "bad sizes nx=%d ny=%d ld=%d (extents <= %d)", nx, ny, ld, PLBM_MAX_EXTENT);
   if (storage != PLBM_F64 && storage != PLBM_F32DEV && storage != PLBM_F16DEV)
     return fail(PLBM_E_INVALID, "unknown storage %d", storage);
   if (!f || !uxa || !uya || !err) return fail(PLBM_E_INVALID, "NULL argument");

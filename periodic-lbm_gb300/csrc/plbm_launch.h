@@ -17,6 +17,9 @@ struct Sweep {
 
 // Threads per block of the per-cell kernels.
 constexpr int kBlock = 256;
+// Blocks of the binary64 field reductions (152 SMs x 8); each writes one
+// partial triple (the staging of plbm_velocity_l2_error_noalloc holds them).
+constexpr int kReduceBlocks = 1216;
 
 // Threads per block for a fused step over `cells` cells: kBlock, or, for a
 // grid with fewer than kBlock cells per SM, the smallest multiple of 32 that

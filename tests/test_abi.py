@@ -88,6 +88,11 @@ def test_extents_above_the_32_bit_cell_limit_are_rejected(lib):
     assert lib.plbm_launch_step(0, 0, 0, 8, 8, big, C.c_void_p(16), C.c_void_p(32), 1.0, 0.25,
                                 None) == _lib.PLBM_E_INVALID
     assert "bad sizes" in _lib.last_error()
+    d, err = np.zeros(4), C.c_double()
+    for nx, ny, ld in ((big, 1, 16), (1, 8, big)):
+        assert lib.plbm_velocity_l2_error_noalloc(0, nx, ny, ld, C.c_void_p(16), d.ctypes.data, d.ctypes.data,
+                                                  C.byref(err), None) == _lib.PLBM_E_INVALID
+        assert "bad sizes" in _lib.last_error()
     assert "#define PLBM_MAX_EXTENT (1 << 30)" in (ROOT / "include" / "plbm_gpu.h").read_text()
 
 

@@ -26,11 +26,11 @@ def _fields(nx, ny, seed):
     return np.ascontiguousarray(ux), np.ascontiguousarray(uy)
 
 
-@pytest.mark.parametrize("storage", ["f64", "f32dev"])
-def test_noalloc_matches_allocating_entry_point_twice(gpu_lib, storage):
+@pytest.mark.parametrize("nx,ny", [(300, 200), (1024, 1024)])  # 1024^2 = the capacity, 2^20 cells
+@pytest.mark.parametrize("storage", ["f64", "f32dev", "f16dev"])
+def test_noalloc_matches_allocating_entry_point_twice(gpu_lib, storage, nx, ny):
     from plbm import LatticeGrid, _lib
     lib = _lib.load()
-    nx, ny = 300, 200
     ux, uy = _fields(nx, ny, 1)
     g = LatticeGrid(nx, ny, storage=storage)
     g.set_relaxation(1.6, 0.25)
@@ -58,3 +58,8 @@ def test_noalloc_rejects_sizes_beyond_its_capacity(gpu_lib):
                                             dummy.ctypes.data, dummy.ctypes.data, C.byref(err), None)
     assert rc == _lib.PLBM_E_INVALID
     assert "exceeds the fixed staging capacity" in _lib.last_error()
+    big = (1 << 30) + 1
+    for nx, ny, ld in ((big, 1, 16), (1, 8, big)):
+        rc = lib.plbm_velocity_l2_error_noalloc(0, nx, ny, ld, C.c_void_p(dummy.ctypes.data),
+                                                dummy.ctypes.data, dummy.ctypes.data, C.byref(err), None)
+        assert rc == _lib.PLBM_E_INVALID and "bad sizes" in _lib.last_error()
