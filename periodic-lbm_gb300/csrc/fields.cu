@@ -9,10 +9,12 @@ namespace {
 
 inline int tiles(int n) { return (n + kBlock - 1) / kBlock; }
 
-// Cell of a (fast, slow) launch: blocks are ftiles per slow line.
-__device__ __forceinline__ bool fs_cell(int ftiles, int nfast, int& fast, int& slow) {
-  slow = blockIdx.x / ftiles;
-  fast = (blockIdx.x - slow * ftiles) * blockDim.x + threadIdx.x;
+// Cell of a (fast, slow) launch: blocks are ftiles per slow line, the first
+// line is slow0 (a slab of slow lines when the work is split).
+__device__ __forceinline__ bool fs_cell(int ftiles, int nfast, int& fast, int& slow, int slow0 = 0) {
+  const int b = blockIdx.x / ftiles;
+  fast = (blockIdx.x - b * ftiles) * blockDim.x + threadIdx.x;
+  slow = slow0 + b;
   return fast < nfast;
 }
 
@@ -51,10 +53,10 @@ __device__ __forceinline__ void cell_moments(const double (&fs)[9], double& rho,
 template <int ST, class L>
 __global__ void __launch_bounds__(kBlock) k_macros(const void* __restrict__ f, double* __restrict__ rho,
                                                   double* __restrict__ ux, double* __restrict__ uy, int nx,
-                                                  int ny, int ld, int ftiles) {
+                                                  int ny, int ld, int ftiles, int slow0) {
   const int nfast = L::x_fast ? nx : ny;
   int fast, slow;
-  if (!fs_cell(ftiles, nfast, fast, slow)) return;
+  if (!fs_cell(ftiles, nfast, fast, slow, slow0)) return;
   const int x = L::x_fast ? fast : slow, y = L::x_fast ? slow : fast;
   double fs[9];
 #pragma unroll
@@ -111,10 +113,10 @@ __global__ void __launch_bounds__(kBlock) k_equilibrium(const double* __restrict
                                                        const double* __restrict__ ux,
                                                        const double* __restrict__ uy, int from_pressure,
                                                        void* __restrict__ f, int nx, int ny, int ld,
-                                                       int ftiles) {
+                                                       int ftiles, int slow0) {
   const int nfast = L::x_fast ? nx : ny;
   int fast, slow;
-  if (!fs_cell(ftiles, nfast, fast, slow)) return;
+  if (!fs_cell(ftiles, nfast, fast, slow, slow0)) return;
   const int x = L::x_fast ? fast : slow, y = L::x_fast ? slow : fast;
   const size_t o = (size_t)fast + (size_t)nfast * slow;
   double feq[9];
@@ -233,11 +235,17 @@ __global__ void __launch_bounds__(kBlock) k_energy_error(const void* __restrict_
 
 cudaError_t macros(int storage, int layout, int nx, int ny, int ld, const void* f, double* rho, double* ux,
                    double* uy, cudaStream_t st) {
+  return macros_range(storage, layout, nx, ny, ld, f, rho, ux, uy, 0, layout ? ny : nx, st);
+}
+
+cudaError_t macros_range(int storage, int layout, int nx, int ny, int ld, const void* f, double* rho, double* ux,
+                         double* uy, int slow0, int slow1, cudaStream_t st) {
   const int nfast = layout ? nx : ny, nslow = layout ? ny : nx;
+  if (slow0 < 0 || slow1 > nslow || slow0 >= slow1) return cudaErrorInvalidValue;
   const int ft = tiles(nfast);
-  const long long blocks = (long long)ft * nslow;
+  const long long blocks = (long long)ft * (slow1 - slow0);
   if (blocks <= 0 || blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
-#define L_(ST, LL) k_macros<ST, LL><<<(unsigned)blocks, kBlock, 0, st>>>(f, rho, ux, uy, nx, ny, ld, ft)
+#define L_(ST, LL) k_macros<ST, LL><<<(unsigned)blocks, kBlock, 0, st>>>(f, rho, ux, uy, nx, ny, ld, ft, slow0)
 #define SW_(LL)                                          \
   switch (storage) {                                     \
     case ST_F64: L_(ST_F64, LL); break;                  \
@@ -254,12 +262,18 @@ cudaError_t macros(int storage, int layout, int nx, int ny, int ld, const void* 
 
 cudaError_t equilibrium(int storage, int layout, int nx, int ny, int ld, const double* rho, const double* ux,
                         const double* uy, int from_pressure, void* f, cudaStream_t st) {
+  return equilibrium_range(storage, layout, nx, ny, ld, rho, ux, uy, from_pressure, f, 0, layout ? ny : nx, st);
+}
+
+cudaError_t equilibrium_range(int storage, int layout, int nx, int ny, int ld, const double* rho, const double* ux,
+                              const double* uy, int from_pressure, void* f, int slow0, int slow1, cudaStream_t st) {
   const int nfast = layout ? nx : ny, nslow = layout ? ny : nx;
+  if (slow0 < 0 || slow1 > nslow || slow0 >= slow1) return cudaErrorInvalidValue;
   const int ft = tiles(nfast);
-  const long long blocks = (long long)ft * nslow;
+  const long long blocks = (long long)ft * (slow1 - slow0);
   if (blocks <= 0 || blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
 #define L_(ST, LL) \
-  k_equilibrium<ST, LL><<<(unsigned)blocks, kBlock, 0, st>>>(rho, ux, uy, from_pressure, f, nx, ny, ld, ft)
+  k_equilibrium<ST, LL><<<(unsigned)blocks, kBlock, 0, st>>>(rho, ux, uy, from_pressure, f, nx, ny, ld, ft, slow0)
 #define SW_(LL)                                          \
   switch (storage) {                                     \
     case ST_F64: L_(ST_F64, LL); break;                  \

@@ -139,6 +139,12 @@ extern "C" int plbm_grid_destroy(plbm_grid_t* g) {
   if (g->spare) cudaFree(g->spare);
   if (g->scratch) cudaFree(g->scratch);
   if (g->step_graph) cudaGraphExecDestroy(g->step_graph);
+  if (g->xfer) {
+    cudaStreamSynchronize(g->xfer);
+    cudaStreamDestroy(g->xfer);
+  }
+  for (cudaEvent_t ev : g->slab_ev)
+    if (ev) cudaEventDestroy(ev);
   if (g->own) cudaStreamDestroy(g->own);
   delete g;
   return PLBM_OK;
@@ -323,6 +329,35 @@ extern "C" int plbm_download(plbm_grid_t* g, double* f_host, int ibuf) {
   return ok();
 }
 
+namespace {
+
+// Large grids move their (ny,nx) moment fields in x-column slabs -- each a
+// contiguous range of the host arrays -- on a second stream, so that the
+// copy of one slab overlaps the kernel of the previous one
+// (set_pdf_to_equilibrium: copy then equilibrium; update_macros: moments
+// then copy).  About 96 MB of fields per slab, at most kMaxSlabs.
+int slab_count(const plbm_grid_t* g) {
+  const size_t n = (size_t)g->nx * g->ny;
+  if (n < ((size_t)1 << 22) || g->nx < 4) return 1;
+  const size_t s = 3 * n * 8 / ((size_t)96 << 20);
+  const size_t lim = (size_t)kMaxSlabs < (size_t)g->nx ? (size_t)kMaxSlabs : (size_t)g->nx;
+  return (int)(s < 2 ? 2 : (s > lim ? lim : s));
+}
+
+int ensure_xfer(plbm_grid_t* g) {
+  if (!g->xfer) CUDA_TRY(cudaStreamCreateWithFlags(&g->xfer, cudaStreamNonBlocking), "transfer stream");
+  for (cudaEvent_t& ev : g->slab_ev)
+    if (!ev) CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "slab event");
+  return PLBM_OK;
+}
+
+inline void slab_bounds(const plbm_grid_t* g, int s, int S, int& x0, int& x1) {
+  x0 = (int)((long long)g->nx * s / S);
+  x1 = (int)((long long)g->nx * (s + 1) / S);
+}
+
+}  // namespace
+
 extern "C" int plbm_set_pdf_to_equilibrium(plbm_grid_t* g, const double* rho, const double* ux, const double* uy) {
   if (int r = check_grid(g)) return r;
   if (!rho || !ux || !uy) return fail(PLBM_E_INVALID, "rho, ux and uy must be non-NULL");
@@ -330,6 +365,29 @@ extern "C" int plbm_set_pdf_to_equilibrium(plbm_grid_t* g, const double* rho, co
   const size_t n = (size_t)g->nx * g->ny;
   if (int r = ensure_scratch(g, 3 * n)) return r;
   double* d = g->scratch;
+  const int S = slab_count(g);
+  if (S > 1) {
+    if (int r = ensure_xfer(g)) return r;
+    // the copies start after the grid's earlier work (which may read the scratch)
+    CUDA_TRY(cudaEventRecord(g->slab_ev[kMaxSlabs], g->stream), "equilibrium order");
+    CUDA_TRY(cudaStreamWaitEvent(g->xfer, g->slab_ev[kMaxSlabs], 0), "equilibrium order");
+    const double* src[3] = {rho, ux, uy};
+    for (int s = 0; s < S; s++) {
+      int x0, x1;
+      slab_bounds(g, s, S, x0, x1);
+      const size_t off = (size_t)x0 * g->ny, cnt = (size_t)(x1 - x0) * g->ny;
+      for (int k = 0; k < 3; k++)
+        CUDA_TRY(cudaMemcpyAsync(d + k * n + off, src[k] + off, cnt * 8, cudaMemcpyHostToDevice, g->xfer),
+                 "upload fields");
+      CUDA_TRY(cudaEventRecord(g->slab_ev[s], g->xfer), "slab event");
+      CUDA_TRY(cudaStreamWaitEvent(g->stream, g->slab_ev[s], 0), "slab wait");
+      CUDA_TRY(equilibrium_range(internal_storage(g->storage), 0, g->nx, g->ny, g->ld, d, d + n, d + 2 * n, 0,
+                                 lattice(g, g->iold), x0, x1, g->stream),
+               "equilibrium kernel");
+    }
+    CUDA_TRY(cudaStreamSynchronize(g->stream), "equilibrium sync");
+    return ok();
+  }
   CUDA_TRY(cudaMemcpyAsync(d, rho, n * 8, cudaMemcpyHostToDevice, g->stream), "upload rho");
   CUDA_TRY(cudaMemcpyAsync(d + n, ux, n * 8, cudaMemcpyHostToDevice, g->stream), "upload ux");
   CUDA_TRY(cudaMemcpyAsync(d + 2 * n, uy, n * 8, cudaMemcpyHostToDevice, g->stream), "upload uy");
@@ -585,6 +643,28 @@ extern "C" int plbm_update_macros(plbm_grid_t* g, double* rho, double* ux, doubl
   if (int r = ensure_scratch(g, 3 * n)) return r;
   double* d = g->scratch;
   // src/fvm_bardow.F90:350-352 reads f(:,:,:,grid%inew)
+  const int S = slab_count(g);
+  if (S > 1) {
+    if (int r = ensure_xfer(g)) return r;
+    double* dst[3] = {rho, ux, uy};
+    for (int s = 0; s < S; s++) {
+      int x0, x1;
+      slab_bounds(g, s, S, x0, x1);
+      CUDA_TRY(macros_range(internal_storage(g->storage), 0, g->nx, g->ny, g->ld, lattice(g, g->inew), d, d + n,
+                            d + 2 * n, x0, x1, g->stream),
+               "moments kernel");
+      CUDA_TRY(cudaEventRecord(g->slab_ev[s], g->stream), "slab event");
+      CUDA_TRY(cudaStreamWaitEvent(g->xfer, g->slab_ev[s], 0), "slab wait");
+      const size_t off = (size_t)x0 * g->ny, cnt = (size_t)(x1 - x0) * g->ny;
+      for (int k = 0; k < 3; k++)
+        if (dst[k])
+          CUDA_TRY(cudaMemcpyAsync(dst[k] + off, d + k * n + off, cnt * 8, cudaMemcpyDeviceToHost, g->xfer),
+                   "download fields");
+    }
+    // the last slab's copies wait for every moments kernel before them
+    CUDA_TRY(cudaStreamSynchronize(g->xfer), "update_macros sync");
+    return ok();
+  }
   CUDA_TRY(macros(internal_storage(g->storage), 0, g->nx, g->ny, g->ld, lattice(g, g->inew), d, d + n, d + 2 * n,
                   g->stream),
            "moments kernel");

@@ -21,6 +21,9 @@ inline int ok() { return PLBM_OK; }
 constexpr int kMaxLattices = 16;
 
 // Device-resident mirror of lattice_grid (src/fvm_bardow.F90:37-69).
+// Most x-column slabs the moment-field transfers are split into.
+constexpr int kMaxSlabs = 16;
+
 struct plbm_grid {
   int nx, ny, ld, nf, storage;
   int kind = PLBM_BGK, math = PLBM_MATH_FMA;
@@ -38,6 +41,10 @@ struct plbm_grid {
   size_t elem_bytes = 8;
   cudaStream_t own = nullptr;  // stream created by the handle
   cudaStream_t stream = nullptr;
+  // Host transfers of set_pdf_to_equilibrium / update_macros on large grids:
+  // a second stream and one event per x-column slab (created on first use).
+  cudaStream_t xfer = nullptr;
+  cudaEvent_t slab_ev[kMaxSlabs + 1] = {};
   double* scratch = nullptr;   // 3*nx*ny doubles + reduction partials
   size_t scratch_elems = 0;
   // Captured step loop of a small grid (plbm_perform_lbm_step) and what it

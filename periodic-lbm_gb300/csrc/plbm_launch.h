@@ -87,6 +87,14 @@ cudaError_t macros(int storage, int layout, int nx, int ny, int ld, const void* 
 cudaError_t equilibrium(int storage, int layout, int nx, int ny, int ld, const double* rho,
                         const double* ux, const double* uy, int from_pressure, void* f,
                         cudaStream_t st);
+// The same over the slow lines [slow0, slow1) only (x columns of the YFast
+// layout): a slab of the grid, for pipelining with host transfers.  The
+// field pointers still address the whole (fast, slow) arrays.
+cudaError_t macros_range(int storage, int layout, int nx, int ny, int ld, const void* f, double* rho,
+                         double* ux, double* uy, int slow0, int slow1, cudaStream_t st);
+cudaError_t equilibrium_range(int storage, int layout, int nx, int ny, int ld, const double* rho,
+                              const double* ux, const double* uy, int from_pressure, void* f, int slow0,
+                              int slow1, cudaStream_t st);
 // binary64 f (YFast) <-> deviation storage conversion: h = f - w_i.
 cudaError_t f64_to_dev(int storage, int nx, int ny, int ld, const double* f, void* h, cudaStream_t st);
 cudaError_t dev_to_f64(int storage, int nx, int ny, int ld, const void* h, double* f, cudaStream_t st);
