@@ -13,8 +13,11 @@
 //   S0 = sum w_q lambda_q, A = sum w_q lambda_q (1 - 4.5 (c_q.u)^2 + 1.5 u^2),
 //   B = sum w_q lambda_q (3 + 9 c_q.u) c_q.
 // The per-cell adjoint arithmetic runs in the storage's type (binary64 for
-// PLBM_F64, binary32 for PLBM_F32DEV); the dL/domega sums are accumulated in
-// binary64, one slot per block, summed in a fixed order at the end.
+// PLBM_F64, binary32 for PLBM_F32DEV): lambda, its weighted sums and mu.  The
+// gradients are accumulated in binary64: each cell's dL/domega term is taken
+// to binary64 and summed over the warp in binary64 into the warp's own slot
+// (the host adds the slots in a fixed order), and dL/du0 is assembled from
+// lambda_0 in binary64 (k_adj_u0).
 #include <cuda_runtime.h>
 
 #include "../../include/plbm_gpu.h"
@@ -74,12 +77,10 @@ __device__ __forceinline__ void cell_state(const R (&g)[9], R& rho, R& ux, R& uy
   }
 }
 
-// Warp sum in the cell arithmetic's type R (binary32 for deviation storage,
-// keeping the kernel off the binary64 pipe).  Each warp then adds its sum to
-// its own binary64 slot: no block barrier, and the host adds the slots in a
+// Warp sum in binary64 of the cells' dL/domega terms.  Each warp adds its sum
+// to its own binary64 slot: no block barrier, and the host adds the slots in a
 // fixed order, so the result does not depend on scheduling.
-template <typename R>
-__device__ __forceinline__ R warp_sum(R v) {
+__device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   return v;
@@ -186,8 +187,8 @@ __global__ void __launch_bounds__(kBlock) k_adj_step(const void* __restrict__ f,
       lo[off[p]] = (E)mu;
     }
   }
-  const R t = warp_sum(part);
-  if ((threadIdx.x & 31) == 0) dom[(size_t)blockIdx.x * (kBlock / 32) + (threadIdx.x >> 5)] += (double)t;
+  const double t = warp_sum((double)part);
+  if ((threadIdx.x & 31) == 0) dom[(size_t)blockIdx.x * (kBlock / 32) + (threadIdx.x >> 5)] += t;
 }
 
 // dL/du0 from lambda_0 and u0.

@@ -124,3 +124,63 @@ def test_adjoint_errors(gpu_lib):
     with pytest.raises(PlbmError):
         a.backward(torch.zeros((2, 16, 16), dtype=torch.float64, device="cuda"))  # no forward yet
     a.close()
+
+
+def config5_problem(n=1024, seed_u=1, seed_t=2):
+    """The adjoint inverse problem at full size: a divergence-free initial
+    velocity of 16 Fourier modes |k| <= 8, amplitudes N(0, 0.01^2) (seed 1),
+    the target from seed 2, tau = 0.8."""
+    import torch
+    from plbm import cases
+    ux, uy = cases.divergence_free_modes(n, 16, 8, 0.01, seed=seed_u)
+    tx, ty = cases.divergence_free_modes(n, 16, 8, 0.01, seed=seed_t)
+    return (torch.tensor(np.stack([ux, uy]), device="cuda"), torch.tensor(np.stack([tx, ty]), device="cuda"))
+
+
+def test_config5_gradient_against_central_differences_full_size(gpu_lib):
+    """1024^2 D2Q9 BGK, T = 2000 steps, checkpoints every 45: dL/du0 and
+    dL/dtau of L = 1/2 |u_T - u*|^2 from the binary64 discrete adjoint against
+    central differences (h = 1e-4) of the binary64 forward model on 32 seeded
+    random components of u0 and on tau, each within 1e-5 relative; then the
+    binary32-storage model's adjoint gradient against the binary64 one (its
+    relative error is printed; the bench records it)."""
+    import torch
+    from plbm.autograd import Adjoint
+    n, T, K, tau, h = 1024, 2000, 45, 0.8, 1e-4
+    u0, tgt = config5_problem(n)
+    a = Adjoint(n, n, T, K, "f64")
+    uT = a.forward(u0, 1.0 / tau)
+    g, dom = a.backward(uT - tgt)
+    gtau = -dom / tau ** 2
+    g = g.cpu().numpy()
+
+    def diff_loss(up, um, tp, tm):
+        # L(+) - L(-) summed as 1/2 (a - b)(a + b - 2 t): no cancellation of the two totals
+        Up, Um = a.forward(up, 1.0 / tp), a.forward(um, 1.0 / tm)
+        return float(torch.sum(0.5 * (Up - Um) * (Up + Um - 2.0 * tgt)))
+
+    rng = np.random.default_rng(2024)
+    worst = 0.0
+    for _ in range(32):
+        c, i, j = int(rng.integers(2)), int(rng.integers(n)), int(rng.integers(n))
+        up, um = u0.clone(), u0.clone()
+        up[c, i, j] += h
+        um[c, i, j] -= h
+        fd = diff_loss(up, um, tau, tau) / (2 * h)
+        rel = abs(fd - g[c, i, j]) / abs(g[c, i, j])
+        worst = max(worst, rel)
+        assert rel <= 1e-5, (c, i, j, fd, g[c, i, j], rel)
+    fd_tau = diff_loss(u0, u0, tau + h, tau - h) / (2 * h)
+    rel_tau = abs(fd_tau - gtau) / abs(gtau)
+    print(f"config 5: worst dL/du0 component error {worst:.2e}, dL/dtau error {rel_tau:.2e}")
+    assert rel_tau <= 1e-5, (fd_tau, gtau)
+    a.close()
+    b = Adjoint(n, n, T, K, "f32dev")
+    uT32 = b.forward(u0, 1.0 / tau)
+    g32, dom32 = b.backward(uT32 - tgt)
+    b.close()
+    g64 = torch.tensor(g, device="cuda")
+    rel32 = float(torch.linalg.norm(g32 - g64) / torch.linalg.norm(g64))
+    rel32_tau = abs(-dom32 / tau ** 2 - gtau) / abs(gtau)
+    print(f"config 5: binary32-storage gradient vs binary64: dL/du0 {rel32:.2e}, dL/dtau {rel32_tau:.2e}")
+    assert rel32 <= 1e-2 and rel32_tau <= 1e-2
