@@ -309,29 +309,46 @@ def mixed_precision_errors(torch, n, tau, checkpoints):
     return out
 
 
-def batched_variant(torch, storage, steps, math="fma"):
+def batched_variant(torch, storage, steps, math="fma", both=True):
+    """Config 4: 512 uneven grids advanced `steps` steps per CUDA-graph launch,
+    with the schedule the autotuner picked; with both=True the other mode
+    (one persistent cooperative launch vs one launch per step) is timed with
+    the same threads too, so the tuner's choice is on record."""
     from plbm import autotune, batched
     b = batched.build_tgv_batch(512, 2024, storage)
     b.set_math(math)
     _, rep = autotune.tune(b, steps=5, reps=1, use_cache=True)
     stream = torch.cuda.Stream()
     b.set_stream(stream.cuda_stream)
-    b.capture(steps)
-    b.launch_graph()
-    b.synchronize()
-    if b.steps % 2:
-        b.capture(steps)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    b.launch_graph()
-    e1.record(stream)
-    b.synchronize()
-    ms = e0.elapsed_time(e1)
     cells = b.cells
-    b.close()
+
+    def timed(sched):
+        b.schedule = batched.Schedule.from_dict(sched)
+        b.capture(steps)
+        b.launch_graph()
+        b.synchronize()
+        if b.steps % 2:
+            b.capture(steps)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        b.launch_graph()
+        e1.record(stream)
+        b.synchronize()
+        return e0.elapsed_time(e1)
+
+    tuned = dict(rep["schedule"])
+    ms = timed(tuned)
     mlups = cells * steps / (ms * 1e-3) / 1e6
+    modes = {("persistent" if tuned["persistent"] else "per_step"): mlups}
+    if both:
+        other = dict(tuned, persistent=1 - int(tuned["persistent"]), ctas_per_sm=0)
+        ms_o = timed(other)
+        modes["persistent" if other["persistent"] else "per_step"] = cells * steps / (ms_o * 1e-3) / 1e6
+    b.close()
     return {"value": mlups, "unit": "MLUPS", "grids": 512, "cells": cells, "math": math, "steps_per_graph": steps,
-            "ms_per_step": ms / steps, "schedule": rep["schedule"], "schedule_cached": rep.get("cached", False),
+            "ms_per_step": ms / steps, "schedule": tuned, "persistent": int(tuned["persistent"]),
+            "schedule_cached": rep.get("cached", False), "mlups_by_mode": modes,
+            "tuner": "fastest of threads x {persistent, per-step} x ty x CTAs/SM on 5-step trials",
             "achieved_gbs": mlups * 1e6 * BYTES_PER_CELL[storage] / 1e9}
 
 
@@ -355,9 +372,21 @@ def adjoint_variant(torch, storage, n=1024, T=2000, K=45):
     torch.cuda.synchronize()
     f_ms, b_ms = e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2])
     mem = a.memory_bytes()
+    g32, dom32 = a.backward(uT - tgt)
     a.close()
-    return {"grid": [n, n], "steps": T, "checkpoint_every": K, "forward_ms": f_ms, "backward_ms": b_ms,
-            "adjoint_over_forward": b_ms / f_ms, "device_GB": mem / 1e9}
+    # the binary64 model's adjoint gradient of the same problem: the binary32
+    # storage gradient's error against it (dL/du0 norm-wise, dL/dtau)
+    a64 = Adjoint(n, n, T, K, "f64")
+    uT64 = a64.forward(u0, 1 / 0.8)
+    g64, dom64 = a64.backward(uT64 - tgt)
+    a64.close()
+    torch.cuda.synchronize()
+    err_u0 = float(torch.linalg.norm(g32 - g64) / torch.linalg.norm(g64))
+    err_tau = abs(dom32 - dom64) / abs(dom64)  # dL/dtau = -dL/domega tau^2: the same relative error
+    return {"grid": [n, n], "steps": T, "checkpoint_every": K, "storage": storage, "forward_ms": f_ms,
+            "backward_ms": b_ms, "adjoint_over_forward": b_ms / f_ms, "device_GB": mem / 1e9,
+            "grad_rel_err_f32_vs_f64": {"du0_l2": err_u0, "dtau": err_tau,
+                                        "against": "binary64 discrete adjoint of the same problem"}}
 
 
 def main() -> None:
@@ -550,13 +579,21 @@ def main() -> None:
                 n, "f32dev", time_grid_steps(torch, n, "f32dev", "bgk", "hybrid", omega, 50, 3, fields), peak)
         var["fp16dev"] = variant_entry(n, "f16dev", time_grid_steps(torch, n, "f16dev", args.kind, "fma", omega, 50, 3,
                                                                    fields), peak)
-        mp = mixed_precision_errors(torch, n, 0.52, (1000,))
+        mp = mixed_precision_errors(torch, n, 0.52, (1000, 5000, 20000))
         var["mixed_precision_l2_vs_f64"] = {
-            "workload": f"shear layer {n}^2 BGK tau=0.52 k=80 delta=0.05 u0=0.04, step 1000 "
-                        "(steps 5000/20000: bench.py --suite mixed)", **mp}
-        var["batched_f64"] = batched_variant(torch, "f64", 50, "hybrid")
-        var["batched_f64_fma"] = batched_variant(torch, "f64", 50)
-        var["batched_f32dev"] = batched_variant(torch, "f32dev", 50)
+            "workload": f"shear layer {n}^2 BGK tau=0.52 k=80 delta=0.05 u0=0.04, velocity L2 error against "
+                        "the binary64 (hybrid) run at steps 1000/5000/20000", **mp,
+            "meets_1e-6": {k: max(v.values()) <= 1e-6 for k, v in mp.items()}}
+        var["fp32dev"]["velocity_l2_vs_f64"] = mp["f32dev/fma"]
+        var["fp32dev"]["meets_1e-6"] = max(mp["f32dev/fma"].values()) <= 1e-6
+        if "fp32dev_compensated" in var:
+            var["fp32dev_compensated"]["velocity_l2_vs_f64"] = mp["f32dev/hybrid"]
+            var["fp32dev_compensated"]["meets_1e-6"] = max(mp["f32dev/hybrid"].values()) <= 1e-6
+        var["fp16dev"]["velocity_l2_vs_f64"] = mp["f16dev/fma"]
+        var["fp16dev"]["meets_1e-6"] = max(mp["f16dev/fma"].values()) <= 1e-6
+        var["batched_f64"] = batched_variant(torch, "f64", 1000, "hybrid")
+        var["batched_f64_fma"] = batched_variant(torch, "f64", 50, both=False)
+        var["batched_f32dev"] = batched_variant(torch, "f32dev", 1000)
         var["adjoint_f32dev"] = adjoint_variant(torch, "f32dev")
         line["variants"] = var
     if not args.no_cpu_baseline:
