@@ -11,22 +11,14 @@
 //               rounded to nearest even, error <= 2^-60)
 //   R, JX, JY = sum F_q, sum cx F_q, sum cy F_q          exact integer sums
 //
-// BGK (src/collision_bgk.F90:58-71, equilibrium src/fvm_bardow.F90:99-126):
-//   populations (bgk_fma): f'_q = fma(k_q RN(omega/36), Y_q, f_q), one binary64
-//     FMA per population, Y_q = 36 (w_q T_q - F_q) / k_q an exact integer
-//     bracket (T_q = R + 3 c_q.J + C_q, the nonlinear terms C_q integer
-//     combinations of three double-float products); described at bgk_fma.
-//   shifted populations h = f - w (the plugin, bgk_fast<true>):
-//     C_q      = rho (4.5 (c_q.u)^2 - 1.5 u^2)           double-float, |C| <~ 1e-2
-//     T_q      = DH + 3 c_q.J + C_q                      integer (C_q's two
-//                                                        binary32 halves added exactly)
-//     h'_q     = fma(omega w_q, T_q, (1 - omega) h_q)    2 binary64 operations
-//   which is f' = (1 - omega) f + omega feq with
-//   feq_q = w_q (rho + 3 c.j + rho (4.5 (c.u)^2 - 1.5 u^2)), j = rho u.  The
-//   rounded constants omega w_q are corrected for in fixed point (mass_k on the
-//   rest population's DH, mom_k on J in the 3 c.J terms) so that the zeroth and
-//   first moments are relaxed with the factors omega sum w and
-//   3 omega sum c_x^2 w of the binary64 weights, as the reference relaxes them.
+// BGK (src/collision_bgk.F90:58-71, equilibrium src/fvm_bardow.F90:99-126),
+// populations and shifted populations h = f - w (the plugin) alike (bgk_fma):
+//   f'_q = fma(k_q RN(omega/36), Y_q, f_q), one binary64 FMA per population,
+//   Y_q = 36 (w_q T_q - F_q) / k_q an exact integer bracket (T_q = R + 3 c_q.J
+//   + C_q, the nonlinear terms C_q integer combinations of three double-float
+//   products).  The zeroth and first moments are relaxed with the factors
+//   omega sum w and 3 omega sum c_x^2 w of the binary64 weights, as the
+//   reference relaxes them (mass_k, mom_k).
 //
 // TRT, incompressible (src/collision_trt.F90:98-152): for a pair p, m = -p
 // with v = c_p.J,
@@ -320,75 +312,6 @@ DF_HD int64_t scale_2m64(int64_t a, int32_t k) {
   return ((int64_t)(int32_t)(a >> 32) * (int64_t)k + (int64_t(1) << 31)) >> 32;
 }
 
-struct Params {
-  double omb;      // 1 - omega
-  double omw[3];   // omega * w for w0, ws, wd (rounded to binary64)
-  int32_t mass_k;  // rest-population correction, mass_correction()
-  int32_t mom_k;   // correction of J in the 3 c.J terms, momentum_correction()
-};
-
-// The nine constants RN(omega w_q) sum to omega (W0 + 4 WS + 4 WD) less
-// delta, the sum of their exact rounding errors fma(omega, w, -RN(omega w)).
-// Uncorrected, the mass of a cell drifts by delta R per step (about 1e-16,
-// 1e-12 over 10,000 steps) where the reference's drifts by its own rounding.
-// The rest population restores it: its linear term gains (delta / omw0) R,
-// formed as scale_2m64(R, mass_k) with mass_k = delta / omw0 2^64.
-inline int32_t mass_correction(double omega, const double (&w)[3], const double (&omw)[3]) {
-  const double d = fma(omega, w[0], -omw[0]) +
-                   4.0 * (fma(omega, w[1], -omw[1]) + fma(omega, w[2], -omw[2]));
-  const double k = ldexp(d / omw[0], 64);
-  return fabs(k) < 0x1p30 ? (int32_t)llrint(k) : 0;
-}
-
-// The same for the first moment: sum_q c_qx RN(omega w_q) 3 c_qx is
-// 3 (2 omws + 4 omwd), short of 3 omega (2 WS + 4 WD) by 3 (2 e_s + 4 e_d);
-// J in the 3 c.J terms is scaled by 1 + mom_k 2^-64.
-inline int32_t momentum_correction(double omega, const double (&w)[3], const double (&omw)[3]) {
-  const double d = 2.0 * fma(omega, w[1], -omw[1]) + 4.0 * fma(omega, w[2], -omw[2]);
-  const double k = ldexp(d / (2.0 * omw[1] + 4.0 * omw[2]), 64);
-  return fabs(k) < 0x1p30 ? (int32_t)llrint(k) : 0;
-}
-
-// Small terms to binary64: the TRT and RR forms add them with df_to_double
-// (bit-assembled halves and one binary64 add); BGK, whose binary64 pipe is
-// already as busy as its issue, adds them to the fixed-point linear term
-// (integer only) and rounds once.
-
-// BGK in the hybrid arithmetic (in place).  On `bad` the populations are
-// left in an unspecified state: the caller evaluates the cell another way.
-// SHIFTED: f holds h = f - w (sim/sim.F90:445-499 semantics, rho = sum h + 1).
-template <bool SHIFTED = false>
-DF_HD void bgk_fast(double (&f)[9], const Params& p, bool& bad) {
-  int64_t F[9];
-  load_cell<SHIFTED>(f, F, bad);
-  const int64_t R = (((F[5] + F[7]) + (F[6] + F[8])) + ((F[1] + F[3]) + (F[2] + F[4]))) + F[0];
-  const int64_t d57 = F[5] - F[7], d86 = F[8] - F[6];
-  const int64_t JX = (d57 + d86) + (F[1] - F[3]);
-  const int64_t JY = (d57 - d86) + (F[2] - F[4]);
-  const df64 rho = df::from_double(fixed_to_double_fast(SHIFTED ? R + kOne : R));
-  const df64 inv = df::recip(rho);
-  const df64 ux = df::mul(fixed_to_df(JX), inv), uy = df::mul(fixed_to_df(JY), inv);
-  const df64 u2_15 = df::mul_f(df::add(df::sqr(ux), df::sqr(uy)), 1.5f);
-  // |C_q| <= rho 9 |u|^2 = 6 rho u2_15 must stay below 2 (NaN fails too)
-  bad |= !(fabsf(rho.hi) * u2_15.hi < 0.3f);
-  {
-    const int64_t c0 = df_to_fixed(df::neg(df::mul(rho, u2_15))) + scale_2m64(R, p.mass_k);
-    f[0] = fma_d(p.omw[0], lin_to_double<SHIFTED>(R + c0), p.omb * f[0]);
-  }
-  const int64_t JXc = JX + scale_2m64(JX, p.mom_k), JYc = JY + scale_2m64(JY, p.mom_k);
-#define PLBM_HY_PAIR(QP, QM, CU, CJ, WI)                                                    \
-  {                                                                                         \
-    const int64_t c = df_to_fixed(df::mul(rho, df::sub(df::mul_f(df::sqr(CU), 4.5f), u2_15))); \
-    const int64_t cj3 = 3 * (CJ);                                                           \
-    f[QP] = fma_d(p.omw[WI], lin_to_double<SHIFTED>(R + cj3 + c), p.omb * f[QP]);           \
-    f[QM] = fma_d(p.omw[WI], lin_to_double<SHIFTED>(R - cj3 + c), p.omb * f[QM]);           \
-  }
-  PLBM_HY_PAIR(1, 3, ux, JXc, 1)
-  PLBM_HY_PAIR(2, 4, uy, JYc, 1)
-  PLBM_HY_PAIR(5, 7, df::add(ux, uy), JXc + JYc, 2)
-  PLBM_HY_PAIR(8, 6, df::sub(ux, uy), JXc - JYc, 2)
-#undef PLBM_HY_PAIR
-}
 
 // ---- conversions shaped for the GB300 pipes ----------------------------------
 // Measured issue rates per SM and clock: integer add/logic/shift and
@@ -585,23 +508,47 @@ DF_HD int64_t to_fixed_nonneg(double d, bool& bad) {
   return r;
 }
 
+// SHIFTED: f holds h = f - w (the plugin's storage, sim/sim.F90:131).  The
+// linear brackets then take DH = sum h = rho - 1 in place of R (the w terms
+// cancel) and the nonlinear terms rho = 1 + DH.  Range for h: |h_0| < 1/2,
+// |h_axis| < 1/8, |h_diag| < 1/16 (biased exponents at most 1021, 1019, 1018),
+// rho >= 1/4 and A + B < 0.2; then |DH| < 1.25, |JX|, |JY| < 1/2,
+// |JX +- JY| < 3/4 and |Y_0| < 10.3, |Y_axis| < 4.9, |Y_diag| < 6.75 (units of
+// 2^59).  Small h are rounded to the fixed point with ties toward +infinity,
+// a bias that leaves the odd moments alone (to_fixed_signed).
+template <bool SHIFTED = false>
 DF_HD void bgk_fma(double (&f)[9], const BgkParams& p, bool& bad) {
   using namespace df;
   int64_t F[9];
-  F[0] = to_fixed_nonneg<1022>(f[0], bad);
-  F[1] = to_fixed_nonneg<1020>(f[1], bad);
-  F[2] = to_fixed_nonneg<1020>(f[2], bad);
-  F[3] = to_fixed_nonneg<1020>(f[3], bad);
-  F[4] = to_fixed_nonneg<1020>(f[4], bad);
-  F[5] = to_fixed_nonneg<1019>(f[5], bad);
-  F[6] = to_fixed_nonneg<1019>(f[6], bad);
-  F[7] = to_fixed_nonneg<1019>(f[7], bad);
-  F[8] = to_fixed_nonneg<1019>(f[8], bad);
+  if constexpr (SHIFTED) {
+    F[0] = to_fixed_signed<1021>(f[0], bad);
+    F[1] = to_fixed_signed<1019>(f[1], bad);
+    F[2] = to_fixed_signed<1019>(f[2], bad);
+    F[3] = to_fixed_signed<1019>(f[3], bad);
+    F[4] = to_fixed_signed<1019>(f[4], bad);
+    F[5] = to_fixed_signed<1018>(f[5], bad);
+    F[6] = to_fixed_signed<1018>(f[6], bad);
+    F[7] = to_fixed_signed<1018>(f[7], bad);
+    F[8] = to_fixed_signed<1018>(f[8], bad);
+  } else {
+    F[0] = to_fixed_nonneg<1022>(f[0], bad);
+    F[1] = to_fixed_nonneg<1020>(f[1], bad);
+    F[2] = to_fixed_nonneg<1020>(f[2], bad);
+    F[3] = to_fixed_nonneg<1020>(f[3], bad);
+    F[4] = to_fixed_nonneg<1020>(f[4], bad);
+    F[5] = to_fixed_nonneg<1019>(f[5], bad);
+    F[6] = to_fixed_nonneg<1019>(f[6], bad);
+    F[7] = to_fixed_nonneg<1019>(f[7], bad);
+    F[8] = to_fixed_nonneg<1019>(f[8], bad);
+  }
+  // R: the zeroth moment of the stored values (rho, or DH when shifted)
   const int64_t R = (((F[5] + F[7]) + (F[6] + F[8])) + ((F[1] + F[3]) + (F[2] + F[4]))) + F[0];
   const int64_t d57 = F[5] - F[7], d86 = F[8] - F[6];
   const int64_t JX = (d57 + d86) + (F[1] - F[3]);
   const int64_t JY = (d57 - d86) + (F[2] - F[4]);
-  const df64 s15 = mul_f(recip(fixed_to_df_x(R)), 1.5f);  // 1.5 / rho
+  const int64_t Rrho = SHIFTED ? R + kOne : R;
+  if constexpr (SHIFTED) bad |= Rrho < (kOne >> 2);
+  const df64 s15 = mul_f(recip(fixed_to_df_x(Rrho)), 1.5f);  // 1.5 / rho
   const df64 jx = fixed_to_df_x(JX), jy = fixed_to_df_x(JY);
   const df64 A = mul_lz(sqr_lz(jx), s15);
   const df64 B = mul_lz(sqr_lz(jy), s15);
@@ -636,7 +583,9 @@ struct TrtParams {
   df64 c1[2];      // les 2w 1.5: coefficient of |j|^2 in sym
 };
 
-// TRT in the hybrid arithmetic (in place); `bad` and SHIFTED as for bgk_fast.
+// TRT in the hybrid arithmetic (in place).  On `bad` the populations are left
+// in an unspecified state (the caller evaluates the cell another way); SHIFTED:
+// f holds h = f - w (sim/sim.F90:445-499 semantics, rho = sum h + 1).
 // The double-float terms use the lazy operations (no renormalisation; 2 %
 // faster, the same agreement with the oracle).
 template <bool SHIFTED = false>
@@ -691,7 +640,7 @@ struct RrParams {
 };
 
 // Recursive regularized collision (src/collision_regularized.F90:72-194) in
-// the hybrid arithmetic (in place); `bad` as for bgk_fast.
+// the hybrid arithmetic (in place); `bad` and SHIFTED as for trt_fast.
 //   f'_q = feq_q + w_q (1 - omega) H_q(a)
 // with feq_q = w_q (T_q + rho NL_q(u)), T_q = R + 3 c_q.J exact, NL_q the
 // second-, third- and fourth-order Hermite terms of the reference's
@@ -773,6 +722,105 @@ DF_HD void rr_fast(double (&f)[9], const RrParams& p, bool& bad) {
   PLBM_HY_RR_PAIR(5, 7, add_lz(d0, m9xy), mul_f_lz(add_lz(mxxy, myyx), 9.0f), JX + JY, 2)
   PLBM_HY_RR_PAIR(6, 8, sub_lz(d0, m9xy), mul_f_lz(sub_lz(mxxy, myyx), 9.0f), JY - JX, 2)
 #undef PLBM_HY_RR_PAIR
+}
+
+// Recursive regularized collision with one binary64 FMA per population.
+// f'_q = w_q (T_q + N_q), T_q = R + 3 c_q.J, N_q the Hermite combination of
+// the six merged coefficients M (rr_fast), so with the fixed-point images of
+// M / 2 (exact halving in double-float), h.., every 36 (f'_q - f_q) / k_q is
+// an integer bracket:
+//   rest      4 Y_0,  Y_0 = 4 R - 9 F_0 - 12 (hxx + hyy) + 18 hxxyy
+//   axis      4 Y_q,  Y_q = T_q - 9 F_q + 6 hxx - 3 hyy - 9 hxxyy -+ 9 hyyx  (x; y alike)
+//   diagonal    Y_q,  Y_q = T_q - 36 F_q + 6 (hxx + hyy) + 18 hxxyy
+//                            +- 18 hxy +- 18 (hxxy +- hyyx)
+// and f'_q = fma(k_q RN(1/36), Y_q 2^-59, f_q).  The Hermite parts of the
+// brackets sum to zero with the weights exactly, as T_q - 36 w_q F_q does; the
+// reference's binary64 weights (sums 1 - 2^-54) take 2^-54 of the mass and
+// momentum each step, restored by p.mass_k / p.mom_k (bgk_fma_params at
+// omega = 1).  Range as bgk_fma, and sum |M / 2| < 0.1 (checked on the
+// binary32 heads): then the Hermite parts add at most 3, 0.9 and 1.8 (units of
+// 2^59) to the rest, axis and diagonal brackets, which stay below 13 x 2^59.
+template <bool SHIFTED = false>
+DF_HD void rr_fma(double (&f)[9], const RrParams& r, const BgkParams& p, bool& bad) {
+  using namespace df;
+  int64_t F[9];
+  if constexpr (SHIFTED) {
+    F[0] = to_fixed_signed<1021>(f[0], bad);
+    F[1] = to_fixed_signed<1019>(f[1], bad);
+    F[2] = to_fixed_signed<1019>(f[2], bad);
+    F[3] = to_fixed_signed<1019>(f[3], bad);
+    F[4] = to_fixed_signed<1019>(f[4], bad);
+    F[5] = to_fixed_signed<1018>(f[5], bad);
+    F[6] = to_fixed_signed<1018>(f[6], bad);
+    F[7] = to_fixed_signed<1018>(f[7], bad);
+    F[8] = to_fixed_signed<1018>(f[8], bad);
+  } else {
+    F[0] = to_fixed_nonneg<1022>(f[0], bad);
+    F[1] = to_fixed_nonneg<1020>(f[1], bad);
+    F[2] = to_fixed_nonneg<1020>(f[2], bad);
+    F[3] = to_fixed_nonneg<1020>(f[3], bad);
+    F[4] = to_fixed_nonneg<1020>(f[4], bad);
+    F[5] = to_fixed_nonneg<1019>(f[5], bad);
+    F[6] = to_fixed_nonneg<1019>(f[6], bad);
+    F[7] = to_fixed_nonneg<1019>(f[7], bad);
+    F[8] = to_fixed_nonneg<1019>(f[8], bad);
+  }
+  const int64_t s57 = F[5] + F[7], s68 = F[6] + F[8];
+  const int64_t sd = s57 + s68;
+  const int64_t R = ((s57 + s68) + ((F[1] + F[3]) + (F[2] + F[4]))) + F[0];
+  const int64_t d57 = F[5] - F[7], d86 = F[8] - F[6];
+  const int64_t JX = (d57 + d86) + (F[1] - F[3]);
+  const int64_t JY = (d57 - d86) + (F[2] - F[4]);
+  const int64_t PXX3 = 3 * ((F[1] + F[3]) + sd) - R;
+  const int64_t PYY3 = 3 * ((F[2] + F[4]) + sd) - R;
+  const int64_t PXY = s57 - s68;
+  const int64_t Rrho = SHIFTED ? R + kOne : R;
+  if constexpr (SHIFTED) bad |= Rrho < (kOne >> 2);
+  const df64 rho = fixed_to_df_x(Rrho);
+  const df64 inv = recip(rho);
+  const df64 jx = fixed_to_df_x(JX), jy = fixed_to_df_x(JY);
+  const df64 ux = mul_lz(jx, inv), uy = mul_lz(jy, inv);
+  const df64 uxx = sqr_lz(ux), uyy = sqr_lz(uy), uxy = mul_lz(ux, uy);
+  const df64 uxxy = mul_lz(uxx, uy), uyyx = mul_lz(uyy, ux), uxxyy = mul_lz(uxx, uyy);
+  const df64 axx = sub_lz(mul_lz(fixed_to_df_x(PXX3), r.third), mul_lz(jx, ux));
+  const df64 ayy = sub_lz(mul_lz(fixed_to_df_x(PYY3), r.third), mul_lz(jy, uy));
+  const df64 axy = sub_lz(fixed_to_df_x(PXY), mul_lz(jx, uy));
+  const df64 axxy = add_lz(mul_pow2(mul_lz(ux, axy), 2.0f), mul_lz(uy, axx));
+  const df64 ayyx = add_lz(mul_pow2(mul_lz(uy, axy), 2.0f), mul_lz(ux, ayy));
+  const df64 axxyy =
+      sub_lz(sub_lz(sub_lz(mul_pow2(add_lz(mul_lz(ux, ayyx), mul_lz(uy, axxy)), 2.0f), mul_lz(uxx, ayy)),
+                    mul_lz(uyy, axx)),
+             mul_pow2(mul_lz(uxy, axy), 4.0f));
+  // M / 2 = (rho (u product) + (1 - omega) a) / 2
+  const df64 mxx = mul_pow2(add_lz(mul_lz(rho, uxx), mul_lz(r.omb, axx)), 0.5f);
+  const df64 myy = mul_pow2(add_lz(mul_lz(rho, uyy), mul_lz(r.omb, ayy)), 0.5f);
+  const df64 mxy = mul_pow2(add_lz(mul_lz(rho, uxy), mul_lz(r.omb, axy)), 0.5f);
+  const df64 mxxy = mul_pow2(add_lz(mul_lz(rho, uxxy), mul_lz(r.omb, axxy)), 0.5f);
+  const df64 myyx = mul_pow2(add_lz(mul_lz(rho, uyyx), mul_lz(r.omb, ayyx)), 0.5f);
+  const df64 mxxyy = mul_pow2(add_lz(mul_lz(rho, uxxyy), mul_lz(r.omb, axxyy)), 0.5f);
+  // sum |M / 2| < 0.1 (NaN fails too)
+  bad |= !(fabsf(mxx.hi) + fabsf(myy.hi) + fabsf(mxy.hi) + fabsf(mxxy.hi) + fabsf(myyx.hi) + fabsf(mxxyy.hi) < 0.1f);
+  const int64_t hxx = df_to_fixed_xu(mxx), hyy = df_to_fixed_xu(myy), hxy = df_to_fixed_xu(mxy);
+  const int64_t hxxy = df_to_fixed_xu(mxxy), hyyx = df_to_fixed_xu(myyx), hxxyy = df_to_fixed_xu(mxxyy);
+  f[0] = fma_d(p.c4, fixed_to_double_tr(4 * R - 9 * F[0] - 12 * (hxx + hyy) + 18 * hxxyy + scale_2m64(R, p.mass_k)),
+               f[0]);
+  const int64_t jx3 = 3 * JX + scale_2m64(JX, p.mom_k), jy3 = 3 * JY + scale_2m64(JY, p.mom_k);
+  const int64_t nx_ = R + 6 * hxx - 3 * hyy - 9 * hxxyy, nxo = 9 * hyyx;
+  const int64_t ny_ = R + 6 * hyy - 3 * hxx - 9 * hxxyy, nyo = 9 * hxxy;
+  f[1] = fma_d(p.c4, fixed_to_double_tr(nx_ + jx3 - nxo - 9 * F[1]), f[1]);
+  f[3] = fma_d(p.c4, fixed_to_double_tr(nx_ - jx3 + nxo - 9 * F[3]), f[3]);
+  f[2] = fma_d(p.c4, fixed_to_double_tr(ny_ + jy3 - nyo - 9 * F[2]), f[2]);
+  f[4] = fma_d(p.c4, fixed_to_double_tr(ny_ - jy3 + nyo - 9 * F[4]), f[4]);
+  // diagonal pairs without the momentum correction (the axis pairs carry it):
+  // q=5 (+x,+y): +18 hxy + 18 (hxxy + hyyx); q=7: +18 hxy - 18 (hxxy + hyyx)
+  // q=6 (-x,+y): -18 hxy + 18 (hxxy - hyyx); q=8: -18 hxy - 18 (hxxy - hyyx)
+  const int64_t dsum = R + 6 * (hxx + hyy) + 18 * hxxyy;
+  const int64_t sp = 3 * (JX + JY), sm = 3 * (JY - JX);
+  const int64_t a5 = 18 * (hxy + hxxy + hyyx), a6 = 18 * (hxy - hxxy + hyyx);
+  f[5] = fma_d(p.c1, fixed_to_double_tr(dsum + sp + a5 - 36 * F[5]), f[5]);
+  f[7] = fma_d(p.c1, fixed_to_double_tr(dsum - sp + 36 * hxy - a5 - 36 * F[7]), f[7]);
+  f[6] = fma_d(p.c1, fixed_to_double_tr(dsum + sm - a6 - 36 * F[6]), f[6]);
+  f[8] = fma_d(p.c1, fixed_to_double_tr(dsum - sm - 36 * hxy + a6 - 36 * F[8]), f[8]);
 }
 
 }  // namespace hy

@@ -96,8 +96,8 @@ df::df64 split_const(double d) {
 // Constants of one hybrid launch: the hybrid operator's and the binary64
 // operator's (for cells outside the hybrid range).
 struct HybridArgs {
-  hy::BgkParams bgk1;  // BGK on populations (bgk_fma)
-  hy::Params bgk;      // BGK on shifted populations (the plugin, bgk_fast<true>)
+  hy::BgkParams bgk1;  // BGK (bgk_fma, populations or shifted populations)
+  hy::BgkParams rr1;   // RR (rr_fma): the one-FMA constants at omega = 1
   hy::TrtParams trt;
   hy::RrParams rr;
   CollParams ref;
@@ -121,11 +121,11 @@ __device__ __noinline__ void hybrid_fallback_cell(const double* __restrict__ src
   g_hybrid_range_flag = 1;
 }
 
-// Resident CTAs per SM the hybrid kernels are compiled for: TRT and RR at 5
-// (register cap 65536 / (256 x 5) = 48; measured best at 8192^2: 4 CTAs made
-// TRT 1 % slower, 6 made RR 4 % slower); BGK (bgk_fma) at 4, 64 registers,
-// which it needs without spills.
-constexpr int hybrid_min_blocks(int kind) { return kind == K_BGK ? 4 : 5; }
+// Resident CTAs per SM the hybrid kernels are compiled for: TRT at 5
+// (register cap 65536 / (256 x 5) = 48; measured best at 8192^2), BGK (bgk_fma)
+// at 4 and RR (rr_fma) at 3, the caps under which they need no spills (64 and
+// 80 registers).
+constexpr int hybrid_min_blocks(int kind) { return kind == K_BGK ? 4 : (kind == K_RR ? 3 : 5); }
 
 // I: index type of the lattice offsets; 32-bit when the whole lattice has
 // fewer than 2^32 elements (one multiply-add per address instead of 64-bit
@@ -152,7 +152,7 @@ __global__ void __launch_bounds__(kBlock, hybrid_min_blocks(KIND)) k_step_hybrid
   f[8] = __ldg(src + (8 * P + cm + yp));
   bool bad = false;
   if (KIND == K_TRT) hy::trt_fast(f, a.trt, bad);
-  else if (KIND == K_RR) hy::rr_fast(f, a.rr, bad);
+  else if (KIND == K_RR) hy::rr_fma(f, a.rr, a.rr1, bad);
   else hy::bgk_fma(f, a.bgk1, bad);
   if (bad) {  // outside the hybrid range: the binary64 operator on the same inputs
     hybrid_fallback_cell<KIND>(src, dst, x, y, nx, ny, ld, a.ref);
@@ -189,7 +189,7 @@ __global__ void __launch_bounds__(kBlock) k_step_scheme_hybrid(const double* __r
   sch::stencil_pull<YFast, TAPS>(src, x, y, nx, ny, ld, st, f);
   bool bad = false;
   if (KIND == K_TRT) hy::trt_fast(f, a.trt, bad);
-  else if (KIND == K_RR) hy::rr_fast(f, a.rr, bad);
+  else if (KIND == K_RR) hy::rr_fma(f, a.rr, a.rr1, bad);
   else hy::bgk_fma(f, a.bgk1, bad);
   if (bad) {
     scheme_fallback_cell<TAPS, KIND>(src, dst, x, y, nx, ny, ld, st, a.ref);
@@ -230,8 +230,8 @@ __global__ void __launch_bounds__(kBlock, hybrid_min_blocks(KIND)) k_push_hybrid
   for (int q = 0; q < 9; q++) f[q] = __ldg(src + ((I)q * P + o));
   bool bad = false;
   if (KIND == K_TRT) hy::trt_fast<true>(f, a.trt, bad);
-  else if (KIND == K_RR) hy::rr_fast<true>(f, a.rr, bad);
-  else hy::bgk_fast<true>(f, a.bgk, bad);
+  else if (KIND == K_RR) hy::rr_fma<true>(f, a.rr, a.rr1, bad);
+  else hy::bgk_fma<true>(f, a.bgk1, bad);
   if (bad) {
     push_fallback_cell<KIND>(src, dst, x, y, nx, ny, ld, a.ref);
     return;
@@ -266,16 +266,6 @@ cudaError_t launch_hybrid(const Sweep& s, unsigned blocks, int bs, int ft, const
 hy::BgkParams hybrid_bgk_params(double omega) {
   const double w[3] = {W0, WS, WD};
   return hy::bgk_fma_params(omega, w);
-}
-
-hy::Params hybrid_params(double omega) {
-  hy::Params p;
-  p.omb = 1.0 - omega;
-  const double w[3] = {W0, WS, WD};
-  for (int i = 0; i < 3; i++) p.omw[i] = omega * w[i];
-  p.mass_k = hy::mass_correction(omega, w, p.omw);
-  p.mom_k = hy::momentum_correction(omega, w, p.omw);
-  return p;
 }
 
 // Constants of the hybrid TRT from the launch's binary64 parameters
@@ -317,7 +307,7 @@ cudaError_t step_pull_df64(int kind, const Sweep& s, const CollParams& cp) {
   if (blocks <= 0 || blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
   HybridArgs a;
   a.bgk1 = hybrid_bgk_params(cp.omega);
-  a.bgk = hybrid_params(cp.omega);
+  a.rr1 = hybrid_bgk_params(1.0);
   a.trt = hybrid_trt_params(cp);
   a.rr = hybrid_rr_params(cp);
   a.ref = cp;
@@ -334,7 +324,7 @@ cudaError_t step_push_hybrid(int kind, const Sweep& s, const CollParams& cp) {
   if (blocks <= 0 || blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
   HybridArgs a;
   a.bgk1 = hybrid_bgk_params(cp.omega);
-  a.bgk = hybrid_params(cp.omega);
+  a.rr1 = hybrid_bgk_params(1.0);
   a.trt = hybrid_trt_params(cp);
   a.rr = hybrid_rr_params(cp);
   a.ref = cp;
@@ -366,7 +356,7 @@ cudaError_t step_scheme_hybrid(int scheme, int kind, const Sweep& s, double dt, 
   const sch::Stencil st = sch::stencil_coefficients(scheme, dt);
   HybridArgs a;
   a.bgk1 = hybrid_bgk_params(cp.omega);
-  a.bgk = hybrid_params(cp.omega);
+  a.rr1 = hybrid_bgk_params(1.0);
   a.trt = hybrid_trt_params(cp);
   a.rr = hybrid_rr_params(cp);
   a.ref = cp;
