@@ -49,8 +49,8 @@ BYTES_PER_CELL = {"f64": 144, "f32dev": 72, "f16dev": 36}
 # DRAM bytes per cell update measured by ncu (dram__bytes_read.sum +
 # dram__bytes_write.sum of one launch / cells) on a 2048^2 capture of the same
 # kernel, scaled by the cell count: profiles/k_step_*_2048_fullset.md.
-NCU_TRAFFIC_PER_CELL = {("f64", "bgk", "hybrid"): 133.1, ("f64", "trt", "hybrid"): 132.4,
-                        ("f64", "rr", "hybrid"): 132.4, ("f64", "bgk", "fma"): 132.4}
+NCU_TRAFFIC_PER_CELL = {("f64", "bgk", "hybrid"): 132.6, ("f64", "trt", "hybrid"): 132.4,
+                        ("f64", "rr", "hybrid"): 133.0, ("f64", "bgk", "fma"): 132.4}
 FALLBACK_HBM_GBS = 6800.0
 
 

@@ -109,7 +109,7 @@ __device__ __forceinline__ void do_tile(const BatchGrid* __restrict__ gp, int2 x
   } else {
     if (HY > 0 || (HY < 0 && __ldg(&gp->hybrid))) {
       bool bad = false;
-      if (kind == K_TRT) hy::trt_fast(f, gp->ht, bad);
+      if (kind == K_TRT) hy::trt_fma(f, gp->ht, bad);
       else hy::bgk_fma(f, gp->hp, bad);
       if (bad) {  // outside the hybrid range: the binary64 operator on the same inputs
         fallback_cell<CG>(src, dst, x, y, gp);
@@ -191,10 +191,11 @@ __global__ void __launch_bounds__(kBatchMaxThreads) k_batch_step(const BatchGrid
 
 // Per-step launch of 128-thread CTAs over the tiles of one collision kind
 // (tile t0 + blockIdx.x), compiled for that kind and arithmetic alone with
-// MINB resident CTAs per SM: the binary64 hybrid BGK tiles fit 56 registers
-// (9 CTAs) and the TRT tiles 72 (7).  One kernel for both kinds needed 97
-// registers, 80 under a cap with spills; the 512-grid binary64 hybrid batch
-// runs 24.5k MLUPS split this way against 20.9k (24.1k with caps 10 / 8).
+// MINB resident CTAs per SM: the binary64 hybrid BGK tiles (bgk_fma) take 64
+// registers (8 CTAs) and the TRT tiles (trt_fma) 72 (7).  One kernel for both
+// kinds needed far more registers than either (97 for the earlier forms, 80
+// under a cap with spills, 20.9k MLUPS on the 512-grid batch against 24.5k
+// split by kind).
 template <class S, typename I, int KIND, int HY, int MINB>
 __global__ void __launch_bounds__(128, MINB) k_batch_kind(const BatchGrid* __restrict__ grids,
                                                          const int2* __restrict__ tile_xy,
@@ -210,7 +211,7 @@ cudaError_t launch_kinds(const BatchLaunch& L, int parity) {
   E* base = static_cast<E*>(L.base);
   const int ntrt = L.ntiles - L.nt_bgk;
   if (L.nt_bgk > 0)
-    k_batch_kind<S, I, K_BGK, HY, (HY > 0 ? 9 : 8)><<<L.nt_bgk, 128, 0, L.stream>>>(L.grids, L.tile_xy, L.tile_grid,
+    k_batch_kind<S, I, K_BGK, HY, 8><<<L.nt_bgk, 128, 0, L.stream>>>(L.grids, L.tile_xy, L.tile_grid,
                                                                                     0, parity, base);
   if (ntrt > 0)
     k_batch_kind<S, I, K_TRT, HY, 7><<<ntrt, 128, 0, L.stream>>>(L.grids, L.tile_xy, L.tile_grid, L.nt_bgk, parity,

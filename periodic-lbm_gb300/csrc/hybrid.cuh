@@ -1,55 +1,37 @@
 // hybrid.cuh -- binary64 collisions with the binary64 pipe reserved for the
-// few operations that need its precision.
+// one operation per population that needs its precision.
 //
 // GB300 issues binary64 at 1/64 of the binary32 rate, so a straight binary64
 // BGK (about 70 FP64 instructions per cell) is bound by the FP64 pipe at ~15 %
-// of HBM bandwidth.  This form keeps every term whose size is O(f) exact or
-// binary64, and moves the rest to the integer and binary32 pipes.
+// of HBM bandwidth.  These forms keep every term whose size is O(f) exact, and
+// do the rest on the integer, XU and binary32 pipes.
 //
 // Common part:
 //   F_q       = f_q * 2^59 as int64 (exact for |f_q| >= 2^-7; below that
-//               rounded to nearest even, error <= 2^-60)
+//               rounded to nearest, error <= 2^-60)
 //   R, JX, JY = sum F_q, sum cx F_q, sum cy F_q          exact integer sums
+//   f'_q      = fma(c_q, Y_q 2^-59, f_q)                  ONE binary64 FMA
+// where Y_q is an integer bracket holding the whole update of population q
+// (the linear part exact, the nonlinear part from double-float or exact
+// 128-bit products taken to the fixed point once), c_q a power-of-two multiple
+// of one rounded relaxation constant, so that the brackets of the nine
+// populations sum to zero with the weights exactly: mass and momentum change
+// only by the nine final roundings, plus the drift the reference's own
+// binary64 weights cause (sums 1 - 2^-54), which is restored in the integers.
 //
-// BGK (src/collision_bgk.F90:58-71, equilibrium src/fvm_bardow.F90:99-126),
-// populations and shifted populations h = f - w (the plugin) alike (bgk_fma):
-//   f'_q = fma(k_q RN(omega/36), Y_q, f_q), one binary64 FMA per population,
-//   Y_q = 36 (w_q T_q - F_q) / k_q an exact integer bracket (T_q = R + 3 c_q.J
-//   + C_q, the nonlinear terms C_q integer combinations of three double-float
-//   products).  The zeroth and first moments are relaxed with the factors
-//   omega sum w and 3 omega sum c_x^2 w of the binary64 weights, as the
-//   reference relaxes them (mass_k, mom_k).
-//
-// TRT, incompressible (src/collision_trt.F90:98-152): for a pair p, m = -p
-// with v = c_p.J,
-//   sym  = les (f_p + f_m - 2w rho) - les 2w (4.5 v^2 - 1.5 |j|^2)
-//   asym = lds (f_p - f_m - 6w v)
-//   f'_p = f_p - sym - asym,   f'_m = f_m - sym + asym
-// The linear brackets are exact integers up to a constant factor:
-//   9 (F_p + F_m) - 2 R   (axis, w = 1/9)    18 (F_p + F_m) - R  (diagonal)
-//   3 (F_p - F_m) - 2 V   (axis)             6 (F_p - F_m) - V   (diagonal)
-// so sym and asym -- the small non-equilibrium parts -- are evaluated in
-// double-float from exact inputs, and each population takes ONE binary64
-// addition: f'_p = f_p + (-sym - asym).  The rest population keeps
-// f'_0 = fma(1 - le, f_0, fma(le 4/9, R, -1.5 le 4/9 |j|^2)).
-//
-// RR (src/collision_regularized.F90:72-194): the non-equilibrium second
-// moments come from exact integer moments (Pxx, Pyy, Pxy), and each population
-// is ONE binary64 FMA, f'_q = fma(w_q, T_q, w_q (rho NL_q + (1 - omega) H_q)),
-// the double-float part formed from six merged Hermite coefficients (rr_fast).
-// TRT and RR use the lazy double-float operations (no renormalisation).
-//
-// Range (TRT, RR and shifted BGK; bgk_fma states its own).  The fast path
-// takes |f_0| < 2, |f_axis| < 1/2, |f_diagonal| < 1/4
-// (biased binary64 exponent at most 1023, 1021, 1020).  Under these limits
-// every integer formed here stays below 16 * 2^59 < 2^63 in magnitude:
-// |R| < 5, |R + 3 c.J| < 11.5, |9 (F_p + F_m) - 2R| < 15,
-// |18 (F_p + F_m) - R| < 13, |3 (F_p - F_m) - 2V| < 3, |6 (F_p - F_m) - V| < 4
-// (in units of 2^59; each bound is the sum over q of |coefficient| x limit).
-// BGK's folded term C_q must also stay below 2 (|T_q| < 13.5), checked once
-// per cell through |C_q| <= 6 rho (1.5 |u|^2).
-// A cell with a population outside the limits reports `bad`; the kernels
-// then evaluate that cell with the binary64 operator instead.
+//   BGK (bgk_fma, src/collision_bgk.F90:58-71 with the equilibrium of
+//     src/fvm_bardow.F90:99-126): the nonlinear terms of all nine populations
+//     are integer combinations of three double-float products.
+//   TRT (trt_fma, incompressible, src/collision_trt.F90:98-152): symmetric
+//     and antisymmetric brackets of each pair, joined by one exact 128-bit
+//     product r D (r = lambda_d / lambda_e scaled); |j|^2 and jx jy exact.
+//   RR (rr_fma, src/collision_regularized.F90:72-194): the six merged Hermite
+//     coefficients of the equilibrium and the regularized part in
+//     double-float, taken to the fixed point at half scale.
+// Each states its range; a cell outside it reports `bad`, and the kernels then
+// evaluate that cell with the binary64 operator of the reference instead.
+// Populations stored shifted (h = f - w, the plugin's storage) take the same
+// forms with DH = sum h = rho - 1 in place of R in the linear brackets.
 #pragma once
 #include "df64.cuh"
 
@@ -60,8 +42,6 @@ using df::df64;
 
 constexpr int kScale = 59;  // fixed-point scale 2^59
 
-// Largest biased binary64 exponent a population may have on the fast path.
-constexpr int kExpRest = 1023, kExpAxis = 1021, kExpDiag = 1020;
 
 DF_HD double fma_d(double a, double b, double c) {
 #ifdef __CUDA_ARCH__
@@ -105,23 +85,6 @@ DF_HD int64_t to_fixed_lim(double d, int emax, bool& bad) {
   return (u >> 63) ? -F : F;
 }
 
-// int64 fixed point (scale 2^59) -> binary64, round to nearest even.
-DF_HD double fixed_to_double(int64_t T) {
-  if (T == 0) return 0.0;
-  const uint64_t s = T < 0 ? 1ull : 0ull;
-  const uint64_t a = s ? (uint64_t)(-T) : (uint64_t)T;
-  const int lz = clz64(a);
-  const uint64_t n = a << lz;  // bit 63 set
-  uint64_t m = n >> 11;
-  const uint64_t rem = n & 0x7FF;
-  if (rem > 0x400 || (rem == 0x400 && (m & 1))) m += 1;
-  int ex = 1086 - lz - kScale;
-  if (m >> 53) {
-    m >>= 1;
-    ex += 1;
-  }
-  return df::u2d((s << 63) | ((uint64_t)ex << 52) | (m & 0xFFFFFFFFFFFFFull));
-}
 
 // int64 fixed point -> double-float (leading 48 bits: hi truncated, lo exact).
 DF_HD df64 fixed_to_df(int64_t T) {
@@ -152,13 +115,6 @@ DF_HD df64 fixed_to_df(int64_t T) {
 #else
 #define PLBM_NOINLINE static __attribute__((noinline))
 #endif
-PLBM_NOINLINE int64_t to_fixed_slow(double d, int emax, int* bad) {
-  bool b = false;
-  const int64_t r = to_fixed_lim(d, emax, b);
-  if (b) *bad = 1;
-  return r;
-}
-PLBM_NOINLINE double fixed_to_double_slow(int64_t T) { return fixed_to_double(T); }
 
 // High word of (hi:lo) << sh, 0 <= sh <= 31.
 DF_HD uint32_t funnel_l(uint32_t lo, uint32_t hi, uint32_t sh) {
@@ -169,55 +125,7 @@ DF_HD uint32_t funnel_l(uint32_t lo, uint32_t hi, uint32_t sh) {
 #endif
 }
 
-// to_fixed_lim for positive f in [2^-7, 2^(EMAX-1022)): one 64-bit shift by
-// 0..EMAX-1016, the same exact value as the general conversion (which handles
-// everything else).
-template <int EMAX>
-DF_HD int64_t to_fixed_fast(double d, bool& bad) {
-  static_assert(EMAX >= 1016 && EMAX <= 1023, "fast-path exponent range");
-  const uint64_t u = df::d2u(d);
-  const uint32_t H = (uint32_t)(u >> 32), L = (uint32_t)u;
-  const uint32_t sh = (H >> 20) - 1016u;  // a set sign bit makes this large
-  if (sh <= (uint32_t)(EMAX - 1016)) {
-    const uint32_t mh = (H & 0xFFFFFu) | 0x100000u;
-    return (int64_t)(((uint64_t)funnel_l(L, mh, sh) << 32) | (uint64_t)(L << sh));
-  }
-  int b = 0;
-  const int64_t r = to_fixed_slow(d, EMAX, &b);
-  if (b) bad = true;
-  return r;
-}
 
-// The nine populations of a cell under the fast-path limits.
-DF_HD void load_fixed(const double (&f)[9], int64_t (&F)[9], bool& bad) {
-  F[0] = to_fixed_fast<kExpRest>(f[0], bad);
-  F[1] = to_fixed_fast<kExpAxis>(f[1], bad);
-  F[2] = to_fixed_fast<kExpAxis>(f[2], bad);
-  F[3] = to_fixed_fast<kExpAxis>(f[3], bad);
-  F[4] = to_fixed_fast<kExpAxis>(f[4], bad);
-  F[5] = to_fixed_fast<kExpDiag>(f[5], bad);
-  F[6] = to_fixed_fast<kExpDiag>(f[6], bad);
-  F[7] = to_fixed_fast<kExpDiag>(f[7], bad);
-  F[8] = to_fixed_fast<kExpDiag>(f[8], bad);
-}
-
-// fixed_to_double for 2^58 <= T < 2^60 (values in [0.5, 2)): a shift by 6 or
-// 7 with round-half-up.  It differs from round-to-nearest-even only on exact
-// ties, a few in a thousand values, by one ulp upward (a bias of order 1e-19
-// relative, far below the rounding of the stored state).
-DF_HD double fixed_to_double_fast(int64_t T) {
-  const uint64_t a = (uint64_t)T;
-  const uint32_t top = (uint32_t)(a >> 58);
-  if (top - 1u <= 2u) {
-    const bool big = top >= 2u;
-    const uint32_t sh = big ? 7u : 6u;
-    uint64_t m = (a + (1ull << (sh - 1u))) >> sh;
-    // m <= 2^53; m == 2^53 carries into the exponent through the add below
-    const uint64_t ex = big ? 1023ull : 1022ull;
-    return df::u2d((ex << 52) + (m - (1ull << 52)));
-  }
-  return fixed_to_double_slow(T);
-}
 
 // ---- shifted populations h = f - w (the plugin path) -------------------------
 // With h in place of f the exact sums give DH = sum h = rho - 1 and the same
@@ -267,44 +175,8 @@ DF_HD double fixed_to_double_any(int64_t T) {
 
 constexpr int64_t kOne = (int64_t)1 << kScale;  // 1.0 in fixed point
 
-template <bool SHIFTED>
-DF_HD void load_cell(const double (&f)[9], int64_t (&F)[9], bool& bad) {
-  if constexpr (SHIFTED) {
-    F[0] = to_fixed_signed<kExpRest>(f[0], bad);
-    F[1] = to_fixed_signed<kExpAxis>(f[1], bad);
-    F[2] = to_fixed_signed<kExpAxis>(f[2], bad);
-    F[3] = to_fixed_signed<kExpAxis>(f[3], bad);
-    F[4] = to_fixed_signed<kExpAxis>(f[4], bad);
-    F[5] = to_fixed_signed<kExpDiag>(f[5], bad);
-    F[6] = to_fixed_signed<kExpDiag>(f[6], bad);
-    F[7] = to_fixed_signed<kExpDiag>(f[7], bad);
-    F[8] = to_fixed_signed<kExpDiag>(f[8], bad);
-  } else {
-    load_fixed(f, F, bad);
-  }
-}
 
-// Linear terms T (R + 3 c.J, R, DH + 3 c.J, ...) to binary64.
-template <bool SHIFTED>
-DF_HD double lin_to_double(int64_t T) {
-  if constexpr (SHIFTED) return fixed_to_double_any(T);
-  else return fixed_to_double_fast(T);
-}
 
-// A binary32 value in the fixed point of scale 2^59, truncated toward zero
-// below 2^-59 (exact for |v| >= 2^-36).  |v| < 2 is the caller's to ensure
-// (larger values saturate the shift and come out wrong, not out of range).
-DF_HD int64_t float_to_fixed(float v) {
-  const uint32_t b = df::f2u(v);
-  const int e = (int)((b >> 23) & 0xFF);
-  const int64_t m = (int64_t)((b & 0x7FFFFFu) | 0x800000u);
-  const int sh = e > 127 ? 36 : e - 91;  // v 2^59 = m 2^(e - 150 + 59)
-  const int64_t F = sh >= 0 ? (m << sh) : (sh > -63 ? (m >> -sh) : 0);
-  return (b >> 31) ? -F : F;
-}
-
-// A normalised double-float in fixed point: the sum of its halves' images.
-DF_HD int64_t df_to_fixed(df64 c) { return float_to_fixed(c.hi) + float_to_fixed(c.lo); }
 
 // a k / 2^64 rounded to nearest, for the constant corrections below
 // (|a| < 2^63, |k| < 2^31; a's low 32 bits do not take part).
@@ -572,161 +444,23 @@ DF_HD void bgk_fma(double (&f)[9], const BgkParams& p, bool& bad) {
   f[8] = fma_d(p.c1, fixed_to_double_tr(dm - sm - 36 * F[8]), f[8]);
 }
 
-// Incompressible TRT constants (index 0: axis pairs, 1: diagonal pairs).
-struct TrtParams {
-  double omb;      // 1 - lambda_e
-  double le_t0;    // lambda_e * 4/9
-  df64 nl0;        // -1.5 lambda_e 4/9: coefficient of |j|^2 in f'_0
-  df64 cs[2];      // les / 9, les / 18: coefficient of the exact symmetric bracket
-  df64 cd[2];      // lds / 3, lds / 6: coefficient of the exact antisymmetric bracket
-  df64 c4[2];      // les 2w 4.5: coefficient of v^2 in sym
-  df64 c1[2];      // les 2w 1.5: coefficient of |j|^2 in sym
-};
-
-// TRT in the hybrid arithmetic (in place).  On `bad` the populations are left
-// in an unspecified state (the caller evaluates the cell another way); SHIFTED:
-// f holds h = f - w (sim/sim.F90:445-499 semantics, rho = sum h + 1).
-// The double-float terms use the lazy operations (no renormalisation; 2 %
-// faster, the same agreement with the oracle).
-template <bool SHIFTED = false>
-DF_HD void trt_fast(double (&f)[9], const TrtParams& p, bool& bad) {
-  int64_t F[9];
-  load_cell<SHIFTED>(f, F, bad);
-  const int64_t R = (((F[5] + F[7]) + (F[6] + F[8])) + ((F[1] + F[3]) + (F[2] + F[4]))) + F[0];
-  const int64_t d57 = F[5] - F[7], d86 = F[8] - F[6];
-  const int64_t JX = (d57 + d86) + (F[1] - F[3]);
-  const int64_t JY = (d57 - d86) + (F[2] - F[4]);
-  const df64 jx = fixed_to_df(JX), jy = fixed_to_df(JY);
-  const df64 j2 = df::add_lz(df::sqr_lz(jx), df::sqr_lz(jy));
-  {
-    const double c0 = df::df_to_double(df::mul_lz(p.nl0, j2));
-    f[0] = fma_d(p.omb, f[0], fma_d(p.le_t0, lin_to_double<SHIFTED>(R), c0));
-  }
-  const df64 c1j2[2] = {df::mul_lz(p.c1[0], j2), df::mul_lz(p.c1[1], j2)};
-  // MS, MD: the exact brackets of the pair; VDF = c_p.j
-#define PLBM_HY_TRT_PAIR(QP, QM, VDF, MS, MD, A)                                            \
-  {                                                                                         \
-    const df64 sym = df::sub_lz(df::mul_lz(p.cs[A], fixed_to_df(MS)),                       \
-                                df::sub_lz(df::mul_lz(p.c4[A], df::sqr_lz(VDF)), c1j2[A])); \
-    const df64 asym = df::mul_lz(p.cd[A], fixed_to_df(MD));                                 \
-    f[QP] = f[QP] + df::df_to_double(df::neg(df::add_lz(sym, asym)));                       \
-    f[QM] = f[QM] + df::df_to_double(df::sub_lz(asym, sym));                                \
-  }
-  {
-    const int64_t s = F[1] + F[3], d = F[1] - F[3];
-    PLBM_HY_TRT_PAIR(1, 3, jx, 9 * s - 2 * R, 3 * d - 2 * JX, 0)
-  }
-  {
-    const int64_t s = F[2] + F[4], d = F[2] - F[4];
-    PLBM_HY_TRT_PAIR(2, 4, jy, 9 * s - 2 * R, 3 * d - 2 * JY, 0)
-  }
-  {
-    const int64_t s = F[5] + F[7], d = F[5] - F[7];
-    PLBM_HY_TRT_PAIR(5, 7, df::add_lz(jx, jy), 18 * s - R, 6 * d - (JX + JY), 1)
-  }
-  {
-    const int64_t s = F[8] + F[6], d = F[8] - F[6];
-    PLBM_HY_TRT_PAIR(8, 6, df::sub_lz(jx, jy), 18 * s - R, 6 * d - (JX - JY), 1)
-  }
-#undef PLBM_HY_TRT_PAIR
-}
-
-// Recursive-regularized constants.
+// Recursive-regularized constants (rr_fma).
 struct RrParams {
-  double w[3];   // 4/9, 1/9, 1/36 in binary64 (final FMA)
+  double w[3];   // 4/9, 1/9, 1/36 in binary64
   df64 wdf[3];   // the same as double-float
   df64 omb;      // 1 - omega
   df64 third;    // 1/3
 };
 
-// Recursive regularized collision (src/collision_regularized.F90:72-194) in
-// the hybrid arithmetic (in place); `bad` and SHIFTED as for trt_fast.
-//   f'_q = feq_q + w_q (1 - omega) H_q(a)
-// with feq_q = w_q (T_q + rho NL_q(u)), T_q = R + 3 c_q.J exact, NL_q the
-// second-, third- and fourth-order Hermite terms of the reference's
-// equilibrium, and the non-equilibrium second moments evaluated from exact
-// integer moments: the equilibrium's second moments are rho u u + rho/3 I
-// (the third- and fourth-order Hermite terms are orthogonal to them on D2Q9),
-// so
-//   a_xx = (3 Pxx - R)/3 - jx ux,  a_yy = (3 Pyy - R)/3 - jy uy,
-//   a_xy = Pxy - jx uy,
-// Pxx = sum cx^2 F, Pyy = sum cy^2 F, Pxy = sum cx cy F.  One binary64 FMA per
-// population: f'_q = fma(w_q, T_q, w_q (rho NL_q + (1 - omega) H_q)), where
-// rho NL_q + (1 - omega) H_q is one Hermite combination of six merged
-// coefficients M = rho (u product) + (1 - omega) a.  The double-float work
-// after the exact moments uses the lazy operations (no renormalisation).
-// Together 37 % faster than separate NL and H terms with renormalised
-// operations, with the same agreement with the oracle over 10,000 steps
-// (rho 2.7e-14, u <= 1.7e-13 at tau 0.6, 0.55, 1/1.9).
-template <bool SHIFTED = false>
-DF_HD void rr_fast(double (&f)[9], const RrParams& p, bool& bad) {
-  using namespace df;
-  int64_t F[9];
-  load_cell<SHIFTED>(f, F, bad);
-  const int64_t s57 = F[5] + F[7], s68 = F[6] + F[8];
-  const int64_t sd = s57 + s68;
-  const int64_t R = ((s57 + s68) + ((F[1] + F[3]) + (F[2] + F[4]))) + F[0];
-  const int64_t d57 = F[5] - F[7], d86 = F[8] - F[6];
-  const int64_t JX = (d57 + d86) + (F[1] - F[3]);
-  const int64_t JY = (d57 - d86) + (F[2] - F[4]);
-  const int64_t PXX3 = 3 * ((F[1] + F[3]) + sd) - R;
-  const int64_t PYY3 = 3 * ((F[2] + F[4]) + sd) - R;
-  const int64_t PXY = s57 - s68;
-  const double Rd = lin_to_double<SHIFTED>(R);
-  const df64 rho = from_double(SHIFTED ? fixed_to_double_fast(R + kOne) : Rd);
-  const df64 inv = recip(rho);
-  const df64 jx = fixed_to_df(JX), jy = fixed_to_df(JY);
-  const df64 ux = mul_lz(jx, inv), uy = mul_lz(jy, inv);
-  const df64 uxx = sqr_lz(ux), uyy = sqr_lz(uy), uxy = mul_lz(ux, uy);
-  const df64 uxxy = mul_lz(uxx, uy), uyyx = mul_lz(uyy, ux), uxxyy = mul_lz(uxx, uyy);
-  // non-equilibrium second moments
-  const df64 axx = sub_lz(mul_lz(fixed_to_df(PXX3), p.third), mul_lz(jx, ux));
-  const df64 ayy = sub_lz(mul_lz(fixed_to_df(PYY3), p.third), mul_lz(jy, uy));
-  const df64 axy = sub_lz(fixed_to_df(PXY), mul_lz(jx, uy));
-  // recursive third and fourth order
-  const df64 axxy = add_lz(mul_pow2(mul_lz(ux, axy), 2.0f), mul_lz(uy, axx));
-  const df64 ayyx = add_lz(mul_pow2(mul_lz(uy, axy), 2.0f), mul_lz(ux, ayy));
-  const df64 axxyy =
-      sub_lz(sub_lz(sub_lz(mul_pow2(add_lz(mul_lz(ux, ayyx), mul_lz(uy, axxy)), 2.0f), mul_lz(uxx, ayy)),
-                    mul_lz(uyy, axx)),
-             mul_pow2(mul_lz(uxy, axy), 4.0f));
-  // rho NL_q and (1 - omega) H_q share their Hermite form (u products in one,
-  // the moments a in the other), so they are combined coefficient by
-  // coefficient first: M = rho (u product) + (1 - omega) a.
-  const df64 mxx = add_lz(mul_lz(rho, uxx), mul_lz(p.omb, axx));
-  const df64 myy = add_lz(mul_lz(rho, uyy), mul_lz(p.omb, ayy));
-  const df64 mxy = add_lz(mul_lz(rho, uxy), mul_lz(p.omb, axy));
-  const df64 mxxy = add_lz(mul_lz(rho, uxxy), mul_lz(p.omb, axxy));
-  const df64 myyx = add_lz(mul_lz(rho, uyyx), mul_lz(p.omb, ayyx));
-  const df64 mxxyy = add_lz(mul_lz(rho, uxxyy), mul_lz(p.omb, axxyy));
-  const df64 s15 = mul_f_lz(add_lz(mxx, myy), -1.5f);  // -1.5 (Mxx + Myy)
-  const df64 t45 = mul_f_lz(mxxyy, 4.5f);              // 4.5 Mxxyy
-  // rest: -1.5 (Mxx + Myy) + 2.25 Mxxyy
-  f[0] = fma_d(p.w[0], Rd, df_to_double(mul_lz(p.wdf[0], add_lz(s15, mul_pow2(t45, 0.5f)))));
-  // pair p, m: w (X +- Y), T = R +- 3 CJ
-#define PLBM_HY_RR_PAIR(QP, QM, X, Y, CJ, WI)                                                 \
-  {                                                                                           \
-    const df64 xx = (X), yy = (Y);                                                            \
-    const int64_t cj3 = 3 * (CJ);                                                             \
-    f[QP] = fma_d(p.w[WI], lin_to_double<SHIFTED>(R + cj3),                                   \
-                  df_to_double(mul_lz(p.wdf[WI], add_lz(xx, yy))));                           \
-    f[QM] = fma_d(p.w[WI], lin_to_double<SHIFTED>(R - cj3),                                   \
-                  df_to_double(mul_lz(p.wdf[WI], sub_lz(xx, yy))));                           \
-  }
-  // axis: 3 Mxx - 1.5 Myy - 4.5 Mxxyy -+ 4.5 Myyx (and x <-> y)
-  PLBM_HY_RR_PAIR(1, 3, sub_lz(add_lz(mul_f_lz(mxx, 4.5f), s15), t45), mul_f_lz(myyx, -4.5f), JX, 1)
-  PLBM_HY_RR_PAIR(2, 4, sub_lz(add_lz(mul_f_lz(myy, 4.5f), s15), t45), mul_f_lz(mxxy, -4.5f), JY, 1)
-  // diagonal: 3 (Mxx + Myy) + 9 Mxxyy +- 9 Mxy, 9 (Mxxy +- Myyx)
-  const df64 d0 = add_lz(mul_pow2(s15, -2.0f), mul_pow2(t45, 2.0f));
-  const df64 m9xy = mul_f_lz(mxy, 9.0f);
-  PLBM_HY_RR_PAIR(5, 7, add_lz(d0, m9xy), mul_f_lz(add_lz(mxxy, myyx), 9.0f), JX + JY, 2)
-  PLBM_HY_RR_PAIR(6, 8, sub_lz(d0, m9xy), mul_f_lz(sub_lz(mxxy, myyx), 9.0f), JY - JX, 2)
-#undef PLBM_HY_RR_PAIR
-}
 
 // Recursive regularized collision with one binary64 FMA per population.
 // f'_q = w_q (T_q + N_q), T_q = R + 3 c_q.J, N_q the Hermite combination of
-// the six merged coefficients M (rr_fast), so with the fixed-point images of
+// the six merged coefficients M = rho (u product) + (1 - omega) a of the
+// second-, third- and fourth-order Hermite terms (the equilibrium's and the
+// regularized non-equilibrium part's, src/collision_regularized.F90:99-194),
+// with a_xx = (3 Pxx - R)/3 - jx ux, a_yy alike, a_xy = Pxy - jx uy from exact
+// integer moments and the recursive third and fourth orders; so with the
+// fixed-point images of
 // M / 2 (exact halving in double-float), h.., every 36 (f'_q - f_q) / k_q is
 // an integer bracket:
 //   rest      4 Y_0,  Y_0 = 4 R - 9 F_0 - 12 (hxx + hyy) + 18 hxxyy
@@ -821,6 +555,125 @@ DF_HD void rr_fma(double (&f)[9], const RrParams& r, const BgkParams& p, bool& b
   f[7] = fma_d(p.c1, fixed_to_double_tr(dsum - sp + 36 * hxy - a5 - 36 * F[7]), f[7]);
   f[6] = fma_d(p.c1, fixed_to_double_tr(dsum + sm - a6 - 36 * F[6]), f[6]);
   f[8] = fma_d(p.c1, fixed_to_double_tr(dsum - sm - 36 * hxy + a6 - 36 * F[8]), f[8]);
+}
+
+// (a b) / 2^sh, 0 < sh < 64, of the exact 128-bit product, rounded to nearest
+// (ties toward +infinity); the caller keeps the result within int64.  Rounding
+// toward -infinity instead biases every product by half a unit in one
+// direction: in the antisymmetric brackets that is a uniform force on the flow
+// (about 3e-19 per step in J), which grew to 2e-12 of the decaying u over
+// 10,000 steps.
+DF_HD int64_t mul_shr(int64_t a, int64_t b, int sh) {
+#ifdef __CUDA_ARCH__
+  int64_t hi = __mul64hi(a, b);
+#else
+  int64_t hi = (int64_t)(((__int128)a * b) >> 64);
+#endif
+  const uint64_t lo = (uint64_t)a * (uint64_t)b;
+  const uint64_t lo2 = lo + (1ull << (sh - 1));
+  hi += (int64_t)(lo2 < lo);
+  return (int64_t)(((uint64_t)hi << (64 - sh)) | (lo2 >> sh));
+}
+
+// Incompressible TRT with one binary64 FMA per population
+// (src/collision_trt.F90:98-152).  With c = RN(lambda_e / 18) and the exact
+// integer brackets of the pairs (axis: weights 1/9, diagonal: 1/36; J2 = |J|^2,
+// XY = JX JY as exact 128-bit products taken to the fixed point)
+//   axis x    Sb = 9 (F_1 + F_3) - 2 R - 6 JX^2 + 3 JY^2,   D = 3 (F_1 - F_3) - 2 JX
+//   diagonal  Sb = 18 (F_5 + F_7) - R - 3 J2 -+ 9 XY,       D = 6 (F_5 - F_7) - (JX +- JY)
+// the reference's sym = les (...) is c Sb (axis) and c/2 Sb (diagonal), its
+// asym the same constants times r D with r = lambda_d / (6 c) (one exact
+// 64 x 64-bit product per pair), so
+//   f'_p = fma(c_k, -(Sb + r D), f_p),  f'_m = fma(c_k, -(Sb - r D), f_m),
+//   f'_0 = fma(2c, 4 R - 6 J2 - 9 F_0, f_0)
+// (c_k = c on the axis pairs, c/2 on the diagonal ones).  The integer brackets
+// sum to zero with the weights; the reference's binary64 weights relax the
+// mass by lambda_e (sum w - 1) R per step (the sum is 1 - 2^-54), restored in
+// the rest bracket (mass_k).  Range: the loads of bgk_fma, and |Sb| < 2^61,
+// |D| < dmax = 2^61 / r (checked), so every bracket stays below 2^62.
+struct TrtFmaParams {
+  double c, c2, ch;  // RN(lambda_e / 18), 2c, c/2
+  int64_t r_fx;      // r = lambda_d / (6c) = r_fx 2^-r_sh
+  int64_t dmax;      // largest |D| with |r D| < 2^61 (0: every cell falls back)
+  int32_t r_sh;
+  int32_t mass_k;    // lambda_e eps_m / (2c) 2^64
+  int32_t mom_k;     // lambda_d eps_j / (2c) 2^64
+};
+
+inline TrtFmaParams trt_fma_params(double lambda_e, double lambda_d, const double (&w)[3]) {
+  TrtFmaParams p;
+  p.c = lambda_e / 18.0;
+  p.c2 = 2.0 * p.c;
+  p.ch = 0.5 * p.c;
+  const double r = lambda_d / (6.0 * p.c);
+  int e = 0;
+  frexp(r, &e);  // r in [2^(e-1), 2^e)
+  int sh = 61 - e;
+  if (sh > 63) sh = 63;
+  if (sh < 1) sh = 1;
+  const double rf = ldexp(r, sh);
+  p.r_sh = sh;
+  p.r_fx = rf < 0x1p62 ? (int64_t)llrint(rf) : 0;
+  p.dmax = r > 0 ? (int64_t)fmin(0x1p61 / r, 0x1p62) : ((int64_t)1 << 62);
+  if (!(rf < 0x1p62) || !(r >= 0)) p.dmax = 0;
+  const double km = ldexp(lambda_e * weight_sum_error(w) / p.c2, 64);
+  const double kj = ldexp(lambda_d * first_moment_error(w) / p.c2, 64);
+  p.mass_k = fabs(km) < 0x1p30 ? (int32_t)llrint(km) : 0;
+  p.mom_k = fabs(kj) < 0x1p30 ? (int32_t)llrint(kj) : 0;
+  return p;
+}
+
+DF_HD int64_t abs64(int64_t v) { return v < 0 ? -v : v; }
+
+template <bool SHIFTED = false>
+DF_HD void trt_fma(double (&f)[9], const TrtFmaParams& p, bool& bad) {
+  int64_t F[9];
+  if constexpr (SHIFTED) {
+    F[0] = to_fixed_signed<1021>(f[0], bad);
+    F[1] = to_fixed_signed<1019>(f[1], bad);
+    F[2] = to_fixed_signed<1019>(f[2], bad);
+    F[3] = to_fixed_signed<1019>(f[3], bad);
+    F[4] = to_fixed_signed<1019>(f[4], bad);
+    F[5] = to_fixed_signed<1018>(f[5], bad);
+    F[6] = to_fixed_signed<1018>(f[6], bad);
+    F[7] = to_fixed_signed<1018>(f[7], bad);
+    F[8] = to_fixed_signed<1018>(f[8], bad);
+  } else {
+    F[0] = to_fixed_nonneg<1022>(f[0], bad);
+    F[1] = to_fixed_nonneg<1020>(f[1], bad);
+    F[2] = to_fixed_nonneg<1020>(f[2], bad);
+    F[3] = to_fixed_nonneg<1020>(f[3], bad);
+    F[4] = to_fixed_nonneg<1020>(f[4], bad);
+    F[5] = to_fixed_nonneg<1019>(f[5], bad);
+    F[6] = to_fixed_nonneg<1019>(f[6], bad);
+    F[7] = to_fixed_nonneg<1019>(f[7], bad);
+    F[8] = to_fixed_nonneg<1019>(f[8], bad);
+  }
+  const int64_t R = (((F[5] + F[7]) + (F[6] + F[8])) + ((F[1] + F[3]) + (F[2] + F[4]))) + F[0];
+  const int64_t d57 = F[5] - F[7], d86 = F[8] - F[6];
+  const int64_t JX = (d57 + d86) + (F[1] - F[3]);
+  const int64_t JY = (d57 - d86) + (F[2] - F[4]);
+  const int64_t X2 = mul_shr(JX, JX, kScale), Y2 = mul_shr(JY, JY, kScale), XY = mul_shr(JX, JY, kScale);
+  const int64_t J2 = X2 + Y2;
+  const int64_t sx = 9 * (F[1] + F[3]) - 2 * R - 6 * X2 + 3 * Y2, dx = 3 * (F[1] - F[3]) - 2 * JX;
+  const int64_t sy = 9 * (F[2] + F[4]) - 2 * R - 6 * Y2 + 3 * X2, dy = 3 * (F[2] - F[4]) - 2 * JY;
+  const int64_t sp = 18 * (F[5] + F[7]) - R - 3 * J2 - 9 * XY, dp = 6 * d57 - (JX + JY);
+  const int64_t sm = 18 * (F[8] + F[6]) - R - 3 * J2 + 9 * XY, dm = 6 * d86 - (JX - JY);
+  const int64_t lim = (int64_t)1 << 61;
+  bad |= (abs64(sx) | abs64(sy) | abs64(sp) | abs64(sm)) >= lim;
+  bad |= (abs64(dx) | abs64(dy) | abs64(dp) | abs64(dm)) >= p.dmax;
+  f[0] = fma_d(p.c2, fixed_to_double_tr(4 * R - 6 * J2 - 9 * F[0] + scale_2m64(R, p.mass_k)), f[0]);
+  const int64_t rx = mul_shr(dx, p.r_fx, p.r_sh) - scale_2m64(JX, p.mom_k);
+  const int64_t ry = mul_shr(dy, p.r_fx, p.r_sh) - scale_2m64(JY, p.mom_k);
+  const int64_t rp = mul_shr(dp, p.r_fx, p.r_sh), rm = mul_shr(dm, p.r_fx, p.r_sh);
+  f[1] = fma_d(p.c, fixed_to_double_tr(-(sx + rx)), f[1]);
+  f[3] = fma_d(p.c, fixed_to_double_tr(rx - sx), f[3]);
+  f[2] = fma_d(p.c, fixed_to_double_tr(-(sy + ry)), f[2]);
+  f[4] = fma_d(p.c, fixed_to_double_tr(ry - sy), f[4]);
+  f[5] = fma_d(p.ch, fixed_to_double_tr(-(sp + rp)), f[5]);
+  f[7] = fma_d(p.ch, fixed_to_double_tr(rp - sp), f[7]);
+  f[8] = fma_d(p.ch, fixed_to_double_tr(-(sm + rm)), f[8]);
+  f[6] = fma_d(p.ch, fixed_to_double_tr(rm - sm), f[6]);
 }
 
 }  // namespace hy

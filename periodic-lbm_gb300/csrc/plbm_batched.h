@@ -13,7 +13,7 @@ constexpr int kBatchMaxThreads = 512;
 struct alignas(16) BatchGrid {
   CollParams p;       // relaxation parameters (grid's omega / TRT magic)
   hy::BgkParams hp;   // the same for the hybrid binary64 BGK (bgk_fma)
-  hy::TrtParams ht;   // ... and TRT
+  hy::TrtFmaParams ht;  // ... and TRT (trt_fma)
   long long off;      // element offset of lattice A; lattice B follows it
   int nx, ny, ld;
   int kind;           // K_BGK or K_TRT
@@ -24,7 +24,7 @@ struct alignas(16) BatchGrid {
 };
 
 hy::BgkParams hybrid_bgk_params(double omega);
-hy::TrtParams hybrid_trt_params(const CollParams& p);
+hy::TrtFmaParams hybrid_trt_params(const CollParams& p);
 
 struct BatchLaunch {
   const BatchGrid* grids;  // device

@@ -98,7 +98,7 @@ df::df64 split_const(double d) {
 struct HybridArgs {
   hy::BgkParams bgk1;  // BGK (bgk_fma, populations or shifted populations)
   hy::BgkParams rr1;   // RR (rr_fma): the one-FMA constants at omega = 1
-  hy::TrtParams trt;
+  hy::TrtFmaParams trt;  // TRT (trt_fma)
   hy::RrParams rr;
   CollParams ref;
 };
@@ -125,7 +125,7 @@ __device__ __noinline__ void hybrid_fallback_cell(const double* __restrict__ src
 // (register cap 65536 / (256 x 5) = 48; measured best at 8192^2), BGK (bgk_fma)
 // at 4 and RR (rr_fma) at 3, the caps under which they need no spills (64 and
 // 80 registers).
-constexpr int hybrid_min_blocks(int kind) { return kind == K_BGK ? 4 : (kind == K_RR ? 3 : 5); }
+constexpr int hybrid_min_blocks(int kind) { return kind == K_RR ? 3 : 4; }
 
 // I: index type of the lattice offsets; 32-bit when the whole lattice has
 // fewer than 2^32 elements (one multiply-add per address instead of 64-bit
@@ -151,7 +151,7 @@ __global__ void __launch_bounds__(kBlock, hybrid_min_blocks(KIND)) k_step_hybrid
   f[7] = __ldg(src + (7 * P + cp + yp));
   f[8] = __ldg(src + (8 * P + cm + yp));
   bool bad = false;
-  if (KIND == K_TRT) hy::trt_fast(f, a.trt, bad);
+  if (KIND == K_TRT) hy::trt_fma(f, a.trt, bad);
   else if (KIND == K_RR) hy::rr_fma(f, a.rr, a.rr1, bad);
   else hy::bgk_fma(f, a.bgk1, bad);
   if (bad) {  // outside the hybrid range: the binary64 operator on the same inputs
@@ -188,7 +188,7 @@ __global__ void __launch_bounds__(kBlock) k_step_scheme_hybrid(const double* __r
   double f[9];
   sch::stencil_pull<YFast, TAPS>(src, x, y, nx, ny, ld, st, f);
   bool bad = false;
-  if (KIND == K_TRT) hy::trt_fast(f, a.trt, bad);
+  if (KIND == K_TRT) hy::trt_fma(f, a.trt, bad);
   else if (KIND == K_RR) hy::rr_fma(f, a.rr, a.rr1, bad);
   else hy::bgk_fma(f, a.bgk1, bad);
   if (bad) {
@@ -229,7 +229,7 @@ __global__ void __launch_bounds__(kBlock, hybrid_min_blocks(KIND)) k_push_hybrid
 #pragma unroll
   for (int q = 0; q < 9; q++) f[q] = __ldg(src + ((I)q * P + o));
   bool bad = false;
-  if (KIND == K_TRT) hy::trt_fast<true>(f, a.trt, bad);
+  if (KIND == K_TRT) hy::trt_fma<true>(f, a.trt, bad);
   else if (KIND == K_RR) hy::rr_fma<true>(f, a.rr, a.rr1, bad);
   else hy::bgk_fma<true>(f, a.bgk1, bad);
   if (bad) {
@@ -270,21 +270,11 @@ hy::BgkParams hybrid_bgk_params(double omega) {
 
 // Constants of the hybrid TRT from the launch's binary64 parameters
 // (le = omega, les = omega/2, lds = lambda_d/2 as the reference forms them).
-hy::TrtParams hybrid_trt_params(const CollParams& cp) {
-  hy::TrtParams p;
-  const double le = cp.omega, les = cp.les, lds = cp.lds;
-  p.omb = 1.0 - le;
-  p.le_t0 = le * TRT_T0;
-  p.nl0 = split_const(-1.5 * p.le_t0);
-  p.cs[0] = split_const(les / 9.0);
-  p.cs[1] = split_const(les / 18.0);
-  p.cd[0] = split_const(lds / 3.0);
-  p.cd[1] = split_const(lds / 6.0);
-  p.c4[0] = split_const(les);          // les 2 (1/9) 4.5
-  p.c4[1] = split_const(les / 4.0);    // les 2 (1/36) 4.5
-  p.c1[0] = split_const(les / 3.0);    // les 2 (1/9) 1.5
-  p.c1[1] = split_const(les / 12.0);   // les 2 (1/36) 1.5
-  return p;
+// Constants of the one-FMA TRT from the launch's binary64 parameters
+// (lambda_e = omega, lambda_d as the reference forms it).
+hy::TrtFmaParams hybrid_trt_params(const CollParams& cp) {
+  const double w[3] = {W0, WS, WD};
+  return hy::trt_fma_params(cp.omega, cp.lambda_d, w);
 }
 
 hy::RrParams hybrid_rr_params(const CollParams& cp) {
