@@ -317,7 +317,7 @@ def batched_variant(torch, storage, steps, math="fma", both=True):
     from plbm import autotune, batched
     b = batched.build_tgv_batch(512, 2024, storage)
     b.set_math(math)
-    _, rep = autotune.tune(b, steps=5, reps=1, use_cache=True)
+    _, rep = autotune.tune(b, steps=10, reps=1, use_cache=True, final_steps=100)
     stream = torch.cuda.Stream()
     b.set_stream(stream.cuda_stream)
     cells = b.cells
@@ -348,7 +348,8 @@ def batched_variant(torch, storage, steps, math="fma", both=True):
     return {"value": mlups, "unit": "MLUPS", "grids": 512, "cells": cells, "math": math, "steps_per_graph": steps,
             "ms_per_step": ms / steps, "schedule": tuned, "persistent": int(tuned["persistent"]),
             "schedule_cached": rep.get("cached", False), "mlups_by_mode": modes,
-            "tuner": "fastest of threads x {persistent, per-step} x ty x CTAs/SM on 5-step trials",
+            "tuner": "fastest of threads x {persistent, per-step} x ty x CTAs/SM on 10-step trials, then the "
+                     "winner against the other mode's best on 100 steps",
             "achieved_gbs": mlups * 1e6 * BYTES_PER_CELL[storage] / 1e9}
 
 

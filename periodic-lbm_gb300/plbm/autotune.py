@@ -6,9 +6,12 @@ the tile height ty for each of the five ny buckets.  The search times short
 runs of the actual batch with CUDA events:
 
 1. for threads in {128, 256, 512} x persistent in {1, 0} with the default ty
-   table, keep the fastest;
+   table, keep the fastest (and the fastest of the other mode);
 2. coordinate descent over the ty of each bucket that holds grids;
-3. resident CTAs per SM in {occupancy maximum, 1, 2, 4}.
+3. resident CTAs per SM in {occupancy maximum, 1, 2, 4};
+4. the winner against the best schedule of the other mode (persistent or per
+   step) on longer runs (final_steps): the persistent launch pays its setup
+   once per run, which short trials overweight.
 
 The winner is cached in a JSON file keyed by the batch signature (grid sizes,
 kinds, storage, collision arithmetic, device), so later runs of the same batch reuse it.  The
@@ -62,7 +65,7 @@ def _time(batch: BatchedGrids, steps: int, reps: int) -> float:
 
 
 def tune(batch: BatchedGrids, steps: int = 10, reps: int = 2, use_cache: bool = True,
-         verbose: bool = False) -> tuple[Schedule, dict]:
+         verbose: bool = False, final_steps: int = 50) -> tuple[Schedule, dict]:
     """Search a schedule for `batch`; sets it and returns (schedule, report)."""
     import torch
     dev = torch.cuda.get_device_name()
@@ -90,6 +93,7 @@ def tune(batch: BatchedGrids, steps: int = 10, reps: int = 2, use_cache: bool = 
 
     base = batch.schedule
     best, best_ms = None, float("inf")
+    by_mode = {}  # persistent -> (schedule, ms) of stage 1
     for threads in (128, 256, 512):
         for persistent in (1, 0):
             s = Schedule.from_dict(base.as_dict())
@@ -99,6 +103,8 @@ def tune(batch: BatchedGrids, steps: int = 10, reps: int = 2, use_cache: bool = 
             ms = trial(s)
             if ms < best_ms:
                 best, best_ms = s, ms
+            if persistent not in by_mode or ms < by_mode[persistent][1]:
+                by_mode[persistent] = (s, ms)
     used = sorted({bucket_of(sp.ny) for sp in batch.specs})
     for b in used:
         for ty in (32, 64, 128, 256, 512):
@@ -115,6 +121,19 @@ def tune(batch: BatchedGrids, steps: int = 10, reps: int = 2, use_cache: bool = 
         ms = trial(s)
         if ms < best_ms:
             best, best_ms = s, ms
+    other = by_mode.get(1 - best.persistent)
+    if other is not None and final_steps > steps:
+        batch.schedule = best
+        ms_best = _time(batch, final_steps, 1)
+        batch.schedule = other[0]
+        ms_other = _time(batch, final_steps, 1)
+        trials.append((other[0].as_dict(), ms_other))
+        if verbose:
+            print(f"  final: {best.as_dict()} -> {ms_best:.4f}, {other[0].as_dict()} -> {ms_other:.4f} ms/step")
+        if ms_other < ms_best:
+            best, best_ms = other[0], ms_other
+        else:
+            best_ms = ms_best
     batch.schedule = best
     report = {"schedule": best.as_dict(), "ms_per_step": best_ms, "trials": len(trials), "device": dev}
     cache[key] = report
