@@ -78,6 +78,8 @@ extern "C" {
  * FDM_BARDOW_ISO    the same with the isotropic differences (FDM_ISO build)
  * FDM_BARDOW_WLS    the same with unweighted least squares (FDM_WLS build)
  * FDM_SOFONEA       stream_fdm_sofonea, src/fvm_bardow.F90:688-886
+ * FDM_BARDOW_WLS_GAUSS_V1 / _V2  stream_fdm_bardow with Gaussian-weighted least
+ *                   squares (FDM_WLS_GAUSS_V1 / V2 builds, :604-644)
  * The finite-volume / finite-difference schemes use grid%dt (set_properties)
  * and run with PLBM_F64 storage, FMA or STRICT arithmetic. */
 #define PLBM_STREAM_LBM            0
@@ -86,6 +88,8 @@ extern "C" {
 #define PLBM_STREAM_FDM_BARDOW_ISO 3
 #define PLBM_STREAM_FDM_BARDOW_WLS 4
 #define PLBM_STREAM_FDM_SOFONEA    5
+#define PLBM_STREAM_FDM_BARDOW_WLS_GAUSS_V1 6
+#define PLBM_STREAM_FDM_BARDOW_WLS_GAUSS_V2 7
 
 typedef struct plbm_grid plbm_grid_t;
 

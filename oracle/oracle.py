@@ -147,7 +147,7 @@ def perform_lbm_step(f2: np.ndarray, ny: int, iold: int, inew: int, kind: int, o
 
 # streaming schemes of src/fvm_bardow.F90 (grid%streaming)
 SCHEMES = {"lbm": 0, "fvm_bardow": 1, "fdm_bardow": 2, "fdm_bardow_iso": 3, "fdm_bardow_wls": 4,
-           "fdm_sofonea": 5}
+           "fdm_sofonea": 5, "fdm_bardow_wls_gauss_v1": 6, "fdm_bardow_wls_gauss_v2": 7}
 
 
 def stream_scheme(fold: np.ndarray, ny: int, scheme: str, dt: float, fnew: np.ndarray | None = None,
@@ -164,6 +164,8 @@ def stream_scheme(fold: np.ndarray, ny: int, scheme: str, dt: float, fnew: np.nd
         L.oref_stream_fvm_bardow(nx, ny, ld, _p(fold), _p(fnew), dt)
     elif s in (2, 3, 4):
         L.oref_stream_fdm_bardow(nx, ny, ld, _p(fold), _p(fnew), dt, s - 2)
+    elif s in (6, 7):
+        L.oref_stream_fdm_bardow(nx, ny, ld, _p(fold), _p(fnew), dt, s - 3)
     else:
         L.oref_stream_fdm_sofonea(nx, ny, ld, _p(fold), _p(fnew), dt)
     return fnew

@@ -595,7 +595,8 @@ void oref_stream_fvm_bardow(int nx, int ny, int ld, const double *fold, double *
 /* stream_fdm_bardow, src/fvm_bardow.F90:526-685.  variant 0: central
  * differences (the default build, :656-663); 1: isotropic differences of
  * Kumar 2004 (FDM_ISO, :645-655); 2: unweighted least squares (FDM_WLS,
- * :597-607). */
+ * :597-607); 3, 4: Gaussian-weighted least squares (FDM_WLS_GAUSS_V1 :604-624,
+ * FDM_WLS_GAUSS_V2 :625-644, the reference's binary64 weights). */
 void oref_stream_fdm_bardow(int nx, int ny, int ld, const double *fold, double *fnew, double dt, int variant)
 {
     const double p2 = 0.5;
@@ -632,6 +633,19 @@ void oref_stream_fdm_bardow(int nx, int ny, int ld, const double *fold, double *
                            one_third * (fse - 2 * fs + fsw);
                     dfyy = one_third * (fne - 2 * fe + fse) + one_third * (fn - 2 * fc + fs) +
                            one_third * (fnw - 2 * fw + fsw);
+                    dfxy = 0.25 * (fne - fnw + fsw - fse);
+                } else if (variant == 3 || variant == 4) {
+                    const int g1 = variant == 3;
+                    const double p1s = g1 ? 0.2880584423829145035434 : 0.3934930210807994210853;
+                    const double p1d = g1 ? 0.1059707788085427065949 : 0.05325348945960039354075;
+                    const double p2c = g1 ? -1.152233769531658458263 : -1.573972084323197018207;
+                    const double p2d1 = g1 ? 0.5761168847658292291314 : 0.7869860421615988421706;
+                    const double p2d2 = g1 ? -0.4238831152341712149578 : -0.2130139578384016019186;
+                    const double p2d = g1 ? 0.2119415576170855242122 : 0.1065069789192007732037;
+                    dfx = p1s * (fe - fw) + p1d * (fne - fnw) + p1d * (fse - fsw);
+                    dfy = p1s * (fn - fs) + p1d * (fne - fse) + p1d * (fnw - fsw);
+                    dfxx = p2c * fc + p2d1 * (fe + fw) + p2d2 * (fn + fs) + p2d * (fne + fnw + fsw + fse);
+                    dfyy = p2c * fc + p2d2 * (fe + fw) + p2d1 * (fn + fs) + p2d * (fne + fnw + fsw + fse);
                     dfxy = 0.25 * (fne - fnw + fsw - fse);
                 } else {
                     dfx = p2 * (fe - fw);
@@ -692,6 +706,7 @@ void oref_perform_step_scheme(int nx, int ny, int ld, double *f, int *iold, int 
         case 1: oref_stream_fvm_bardow(nx, ny, ld, fo, fn, dt); break;
         case 2: case 3: case 4: oref_stream_fdm_bardow(nx, ny, ld, fo, fn, dt, scheme - 2); break;
         case 5: oref_stream_fdm_sofonea(nx, ny, ld, fo, fn, dt); break;
+        case 6: case 7: oref_stream_fdm_bardow(nx, ny, ld, fo, fn, dt, scheme - 3); break;
         default: oref_lbm_stream(nx, ny, ld, fo, fn); break;
         }
         switch (kind) {

@@ -269,7 +269,7 @@ extern "C" int plbm_set_time_step(plbm_grid_t* g, double dt) {
 
 extern "C" int plbm_set_streaming(plbm_grid_t* g, int scheme) {
   if (int r = check_grid(g)) return r;
-  if (scheme < PLBM_STREAM_LBM || scheme > PLBM_STREAM_FDM_SOFONEA)
+  if (scheme < PLBM_STREAM_LBM || scheme > PLBM_STREAM_FDM_BARDOW_WLS_GAUSS_V2)
     return fail(PLBM_E_INVALID, "unknown streaming scheme %d", scheme);
   g->streaming = scheme;
   return PLBM_OK;

@@ -24,7 +24,7 @@
 namespace plbm {
 namespace sch {
 
-enum { FVM = 1, FDM = 2, FDM_ISO = 3, FDM_WLS = 4, SOFONEA = 5 };
+enum { FVM = 1, FDM = 2, FDM_ISO = 3, FDM_WLS = 4, SOFONEA = 5, FDM_WLS_G1 = 6, FDM_WLS_G2 = 7 };
 enum { C = 0, E = 1, N = 2, W = 3, S = 4, NE = 5, NW = 6, SW = 7, SE = 8 };
 
 // Neighbour offsets of the order above.
@@ -86,6 +86,23 @@ SCH_HD double scheme_value(int scheme, const double (&v)[9], int q, double dt) {
     dfy = one_sixth * ((fne - fse) + (fn - fs) + (fnw - fsw));
     dfxx = one_third * (fne - 2 * fn + fnw) + one_third * (fe - 2 * fc + fw) + one_third * (fse - 2 * fs + fsw);
     dfyy = one_third * (fne - 2 * fe + fse) + one_third * (fn - 2 * fc + fs) + one_third * (fnw - 2 * fw + fsw);
+    dfxy = 0.25 * (fne - fnw + fsw - fse);
+  } else if (scheme == FDM_WLS_G1 || scheme == FDM_WLS_G2) {
+    // Gaussian-weighted least squares: FDM_WLS_GAUSS_V1 (weight scaled to the
+    // farthest node, src/fvm_bardow.F90:604-624) and FDM_WLS_GAUSS_V2 (to the
+    // closest node, :625-644); the fitted weights are the reference's binary64
+    // constants.
+    const bool v1 = scheme == FDM_WLS_G1;
+    const double p1s = v1 ? 0.2880584423829145035434 : 0.3934930210807994210853;
+    const double p1d = v1 ? 0.1059707788085427065949 : 0.05325348945960039354075;
+    const double p2c = v1 ? -1.152233769531658458263 : -1.573972084323197018207;
+    const double p2d1 = v1 ? 0.5761168847658292291314 : 0.7869860421615988421706;
+    const double p2d2 = v1 ? -0.4238831152341712149578 : -0.2130139578384016019186;
+    const double p2d = v1 ? 0.2119415576170855242122 : 0.1065069789192007732037;
+    dfx = p1s * (fe - fw) + p1d * (fne - fnw) + p1d * (fse - fsw);
+    dfy = p1s * (fn - fs) + p1d * (fne - fse) + p1d * (fnw - fsw);
+    dfxx = p2c * fc + p2d1 * (fe + fw) + p2d2 * (fn + fs) + p2d * (fne + fnw + fsw + fse);
+    dfyy = p2c * fc + p2d2 * (fe + fw) + p2d1 * (fn + fs) + p2d * (fne + fnw + fsw + fse);
     dfxy = 0.25 * (fne - fnw + fsw - fse);
   } else {
     dfx = 0.5 * (fe - fw);

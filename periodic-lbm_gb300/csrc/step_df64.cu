@@ -339,7 +339,7 @@ cudaError_t step_push_hybrid(int kind, const Sweep& s, const CollParams& cp) {
 
 cudaError_t step_scheme_hybrid(int scheme, int kind, const Sweep& s, double dt, const CollParams& cp) {
   if (kind != K_BGK && kind != K_TRT && kind != K_RR) return cudaErrorNotSupported;
-  if (scheme < sch::FVM || scheme > sch::SOFONEA) return cudaErrorInvalidValue;
+  if (scheme < sch::FVM || scheme > sch::FDM_WLS_G2) return cudaErrorInvalidValue;
   const int ft = (s.ny + kBlock - 1) / kBlock;
   const long long blocks = (long long)ft * s.nx;
   if (blocks <= 0 || blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;

@@ -239,6 +239,8 @@ cudaError_t stream_scheme_f64(int scheme, const Sweep& s, double dt) {
     case sch::FDM_ISO: k_stream_scheme<sch::FDM_ISO><<<nb, kBlock, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft, dt); break;
     case sch::FDM_WLS: k_stream_scheme<sch::FDM_WLS><<<nb, kBlock, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft, dt); break;
     case sch::SOFONEA: k_stream_scheme<sch::SOFONEA><<<nb, kBlock, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft, dt); break;
+    case sch::FDM_WLS_G1: k_stream_scheme<sch::FDM_WLS_G1><<<nb, kBlock, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft, dt); break;
+    case sch::FDM_WLS_G2: k_stream_scheme<sch::FDM_WLS_G2><<<nb, kBlock, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft, dt); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
@@ -261,7 +263,7 @@ cudaError_t step_scheme_f64(int scheme, int kind, const Sweep& s, double dt, con
     case K_BGKI: k_step_scheme<SC, K_BGKI><<<nb, kBlock, 0, s.stream>>>(a, b, s.nx, s.ny, s.ld, ft, st, p); break; \
     default: return cudaErrorInvalidValue;                                                                    \
   }
-  if (scheme < sch::FVM || scheme > sch::SOFONEA) return cudaErrorInvalidValue;
+  if (scheme < sch::FVM || scheme > sch::FDM_WLS_G2) return cudaErrorInvalidValue;
   switch (sch::taps_of(scheme)) {
     case sch::TAPS_LINE: PLBM_SCH_KIND(sch::TAPS_LINE) break;
     case sch::TAPS_AXIS3: PLBM_SCH_KIND(sch::TAPS_AXIS3) break;

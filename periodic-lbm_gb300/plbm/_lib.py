@@ -34,7 +34,7 @@ MATHS = {"fma": MATH_FMA, "strict": MATH_STRICT, "hybrid": MATH_HYBRID, "df64": 
 
 # streaming schemes (grid%streaming)
 SCHEMES = {"lbm": 0, "fvm_bardow": 1, "fdm_bardow": 2, "fdm_bardow_iso": 3, "fdm_bardow_wls": 4,
-           "fdm_sofonea": 5}
+           "fdm_sofonea": 5, "fdm_bardow_wls_gauss_v1": 6, "fdm_bardow_wls_gauss_v2": 7}
 
 F16_SCALE_LOG2 = 15
 

@@ -112,9 +112,10 @@ class LatticeGrid:
 
     @streaming.setter
     def streaming(self, scheme) -> None:
-        """grid%streaming => lbm_stream | stream_fvm_bardow | stream_fdm_bardow[_iso|_wls] |
-        stream_fdm_sofonea ("lbm", "fvm_bardow", "fdm_bardow", "fdm_bardow_iso",
-        "fdm_bardow_wls", "fdm_sofonea")."""
+        """grid%streaming => lbm_stream | stream_fvm_bardow |
+        stream_fdm_bardow[_iso|_wls|_wls_gauss_v1|_wls_gauss_v2] | stream_fdm_sofonea
+        ("lbm", "fvm_bardow", "fdm_bardow", "fdm_bardow_iso", "fdm_bardow_wls",
+        "fdm_bardow_wls_gauss_v1", "fdm_bardow_wls_gauss_v2", "fdm_sofonea")."""
         v = _lib.SCHEMES[scheme] if isinstance(scheme, str) else int(scheme)
         check(self._lib.plbm_set_streaming(self.handle, v))
         self._streaming = v

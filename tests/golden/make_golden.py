@@ -300,6 +300,20 @@ def stream_fdm(f, ny, dt, variant):
             dfxx = t12 * (fne - 2 * fn + fnw) + f6 * (fe - 2 * fc + fw) + t12 * (fse - 2 * fs + fsw)
             dfyy = t12 * (fne - 2 * fe + fse) + f6 * (fn - 2 * fc + fs) + t12 * (fnw - 2 * fw + fsw)
             dfxy = 0.25 * (fne - fse - fnw + fsw)
+        elif variant in ("gauss_v1", "gauss_v2"):
+            # Gaussian-weighted least squares, the reference's binary64 weights
+            # (src/fvm_bardow.F90:604-644)
+            w = {"gauss_v1": (0.2880584423829145035434, 0.1059707788085427065949, -1.152233769531658458263,
+                              0.5761168847658292291314, -0.4238831152341712149578, 0.2119415576170855242122),
+                 "gauss_v2": (0.3934930210807994210853, 0.05325348945960039354075, -1.573972084323197018207,
+                              0.7869860421615988421706, -0.2130139578384016019186, 0.1065069789192007732037)}[variant]
+            a1, a2, b0, b1, b2, b3 = w
+            dfx = a1 * (fe - fw) + a2 * (fne - fnw) + a2 * (fse - fsw)
+            dfy = a1 * (fn - fs) + a2 * (fne - fse) + a2 * (fnw - fsw)
+            corners = fne + fnw + fsw + fse
+            dfxx = b0 * fc + b1 * (fe + fw) + b2 * (fn + fs) + b3 * corners
+            dfyy = b0 * fc + b2 * (fe + fw) + b1 * (fn + fs) + b3 * corners
+            dfxy = 0.25 * (fne - fnw + fsw - fse)
         elif variant == "wls":
             dfx = s6 * ((fne - fnw) + (fe - fw) + (fse - fsw))
             dfy = s6 * ((fne - fse) + (fn - fs) + (fnw - fsw))
@@ -409,6 +423,8 @@ def main():
                          ("fdm_bardow", lambda f: stream_fdm(f, ny, 0.7, "")),
                          ("fdm_bardow_iso", lambda f: stream_fdm(f, ny, 0.7, "iso")),
                          ("fdm_bardow_wls", lambda f: stream_fdm(f, ny, 0.7, "wls")),
+                         ("fdm_bardow_wls_gauss_v1", lambda f: stream_fdm(f, ny, 0.7, "gauss_v1")),
+                         ("fdm_bardow_wls_gauss_v2", lambda f: stream_fdm(f, ny, 0.7, "gauss_v2")),
                          ("fdm_sofonea", lambda f: stream_sofonea(f, ny, 0.7))]:
             g[f"schemes_{tag}_{name}"] = fn(f0)
             f = f0.copy()

@@ -11,7 +11,8 @@ from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
 
-SCHEMES = ["fvm_bardow", "fdm_bardow", "fdm_bardow_iso", "fdm_bardow_wls", "fdm_sofonea"]
+SCHEMES = ["fvm_bardow", "fdm_bardow", "fdm_bardow_iso", "fdm_bardow_wls", "fdm_bardow_wls_gauss_v1",
+           "fdm_bardow_wls_gauss_v2", "fdm_sofonea"]
 KIND = {"bgk": O.BGK, "trt": O.TRT, "rr": O.RR}
 
 

@@ -202,13 +202,14 @@ def test_taylor_green_reference_loop_quirk():
     assert np.all(c[1][:, 4:] == 0.0) and np.any(c[1][:, :4] != 0.0)
 
 
-SCHEME_NAMES = ["fvm_bardow", "fdm_bardow", "fdm_bardow_iso", "fdm_bardow_wls", "fdm_sofonea"]
+SCHEME_NAMES = ["fvm_bardow", "fdm_bardow", "fdm_bardow_iso", "fdm_bardow_wls", "fdm_bardow_wls_gauss_v1",
+                "fdm_bardow_wls_gauss_v2", "fdm_sofonea"]
 
 
 @pytest.mark.parametrize("nx,ny", [(17, 13), (16, 16)])
 @pytest.mark.parametrize("scheme", SCHEME_NAMES)
 def test_streaming_schemes_match_golden(golden, nx, ny, scheme):
-    """stream_fvm_bardow / stream_fdm_bardow (3 variants) / stream_fdm_sofonea
+    """stream_fvm_bardow / stream_fdm_bardow (5 variants) / stream_fdm_sofonea
     (src/fvm_bardow.F90:393-886): the C oracle against the independent numpy
     restatement, one application and 5 steps with BGK, bit for bit."""
     tag = f"schemes_{nx}x{ny}"
