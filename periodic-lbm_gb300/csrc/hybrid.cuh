@@ -514,11 +514,12 @@ DF_HD void rr_fma(double (&f)[9], const RrParams& r, const BgkParams& p, bool& b
   const df64 inv = recip(rho);
   const df64 jx = fixed_to_df_x(JX), jy = fixed_to_df_x(JY);
   const df64 ux = mul_lz(jx, inv), uy = mul_lz(jy, inv);
+  // rho times the velocity products: rho ux^2 = jx ux, rho ux uy = jx uy, ...
+  const df64 qxx = mul_lz(jx, ux), qyy = mul_lz(jy, uy), qxy = mul_lz(jx, uy);
   const df64 uxx = sqr_lz(ux), uyy = sqr_lz(uy), uxy = mul_lz(ux, uy);
-  const df64 uxxy = mul_lz(uxx, uy), uyyx = mul_lz(uyy, ux), uxxyy = mul_lz(uxx, uyy);
-  const df64 axx = sub_lz(mul_lz(fixed_to_df_x(PXX3), r.third), mul_lz(jx, ux));
-  const df64 ayy = sub_lz(mul_lz(fixed_to_df_x(PYY3), r.third), mul_lz(jy, uy));
-  const df64 axy = sub_lz(fixed_to_df_x(PXY), mul_lz(jx, uy));
+  const df64 axx = sub_lz(mul_lz(fixed_to_df_x(PXX3), r.third), qxx);
+  const df64 ayy = sub_lz(mul_lz(fixed_to_df_x(PYY3), r.third), qyy);
+  const df64 axy = sub_lz(fixed_to_df_x(PXY), qxy);
   const df64 axxy = add_lz(mul_pow2(mul_lz(ux, axy), 2.0f), mul_lz(uy, axx));
   const df64 ayyx = add_lz(mul_pow2(mul_lz(uy, axy), 2.0f), mul_lz(ux, ayy));
   const df64 axxyy =
@@ -526,12 +527,12 @@ DF_HD void rr_fma(double (&f)[9], const RrParams& r, const BgkParams& p, bool& b
                     mul_lz(uyy, axx)),
              mul_pow2(mul_lz(uxy, axy), 4.0f));
   // M / 2 = (rho (u product) + (1 - omega) a) / 2
-  const df64 mxx = mul_pow2(add_lz(mul_lz(rho, uxx), mul_lz(r.omb, axx)), 0.5f);
-  const df64 myy = mul_pow2(add_lz(mul_lz(rho, uyy), mul_lz(r.omb, ayy)), 0.5f);
-  const df64 mxy = mul_pow2(add_lz(mul_lz(rho, uxy), mul_lz(r.omb, axy)), 0.5f);
-  const df64 mxxy = mul_pow2(add_lz(mul_lz(rho, uxxy), mul_lz(r.omb, axxy)), 0.5f);
-  const df64 myyx = mul_pow2(add_lz(mul_lz(rho, uyyx), mul_lz(r.omb, ayyx)), 0.5f);
-  const df64 mxxyy = mul_pow2(add_lz(mul_lz(rho, uxxyy), mul_lz(r.omb, axxyy)), 0.5f);
+  const df64 mxx = mul_pow2(add_lz(qxx, mul_lz(r.omb, axx)), 0.5f);
+  const df64 myy = mul_pow2(add_lz(qyy, mul_lz(r.omb, ayy)), 0.5f);
+  const df64 mxy = mul_pow2(add_lz(qxy, mul_lz(r.omb, axy)), 0.5f);
+  const df64 mxxy = mul_pow2(add_lz(mul_lz(qxx, uy), mul_lz(r.omb, axxy)), 0.5f);
+  const df64 myyx = mul_pow2(add_lz(mul_lz(qyy, ux), mul_lz(r.omb, ayyx)), 0.5f);
+  const df64 mxxyy = mul_pow2(add_lz(mul_lz(qxx, uyy), mul_lz(r.omb, axxyy)), 0.5f);
   // sum |M / 2| < 0.1 (NaN fails too)
   bad |= !(fabsf(mxx.hi) + fabsf(myy.hi) + fabsf(mxy.hi) + fabsf(mxxy.hi) + fabsf(myyx.hi) + fabsf(mxxyy.hi) < 0.1f);
   const int64_t hxx = df_to_fixed_xu(mxx), hyy = df_to_fixed_xu(myy), hxy = df_to_fixed_xu(mxy);
