@@ -13,14 +13,16 @@ straight binary64 kernel is measured beside it ("variants.fp64_native").
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                     [--n 8192] [--kind bgk|trt|rr] [--storage f64|f32dev|f16dev]
                     [--math fma|strict|hybrid] [--no-variants] [--no-cpu-baseline]
-                    [--suite mixed]
+                    [--suite mixed|fields]
 
 Prints one JSON line (rank 0).  --impl reference times the reference's
 algorithm on the host cores instead: the C restatement of the Fortran
 (two passes per step, stream then collide, OpenMP over all host threads).
 --suite mixed runs the mixed-precision study (shear layer, 8192^2, tau 0.52,
 velocity L2 error of binary32/binary16 deviation storage against binary64 at
-steps 1000/5000/20000) and prints its own JSON line.
+steps 1000/5000/20000) and prints its own JSON line; --suite fields times the
+two field kernels around the job (equilibrium, moments) on device-resident
+fields, integer forms and reference expressions ("variants.field_kernels").
 """
 from __future__ import annotations
 
@@ -210,6 +212,54 @@ def time_grid_steps(torch, n, storage, kind, math_mode, omega, steps, warmup, fi
     ms = e0.elapsed_time(e1)
     g.close()
     return ms / steps
+
+
+def field_kernels_variant(torch, n, fields, peak, reps=5):
+    """Device time of the two field kernels around the job on device-resident
+    (ny,nx) fields: plbm_equilibrium_device (24 B in, 72 B out per cell) and
+    plbm_macros_device (72 B in, 24 B out), per arithmetic: the integer forms
+    of hybrid grids and the reference's binary64 expressions (FMA grids).
+    CUDA events on the grid's stream, median of reps; inputs exceed L2."""
+    from plbm import LatticeGrid, _lib
+    lib = _lib.load()
+    stream = torch.cuda.Stream()
+    dev = [torch.from_numpy(np.ascontiguousarray(a)).to("cuda") for a in fields]
+    out = [torch.empty_like(dev[0]) for _ in range(3)]
+    bytes_per_cell = 96.0
+    res = {"workload": f"{n}^2 cells, rho/ux/uy (ny,nx) binary64 on the device <-> one binary64 lattice",
+           "algorithmic_bytes_per_cell": bytes_per_cell}
+    for mm in ("hybrid", "fma"):
+        g = LatticeGrid(n, n, collision="bgk", math=mm)
+        g.set_stream(stream.cuda_stream)
+        times = {}
+        for name in ("equilibrium", "macros"):
+            def launch():
+                if name == "equilibrium":
+                    _lib.check(lib.plbm_equilibrium_device(g.handle, g.iold, *(d.data_ptr() for d in dev)))
+                else:
+                    _lib.check(lib.plbm_macros_device(g.handle, g.iold, *(o.data_ptr() for o in out)))
+            launch()
+            torch.cuda.synchronize()
+            ts = []
+            for _ in range(reps):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                launch()
+                e1.record(stream)
+                torch.cuda.synchronize()
+                ts.append(e0.elapsed_time(e1))
+            ms = float(np.median(ts))
+            gbs = bytes_per_cell * n * n / (ms * 1e-3) / 1e9
+            times[name] = {"ms": ms, "achieved_gbs": gbs, "frac_of_measured_hbm": gbs / peak}
+        if mm == "hybrid":
+            # moments of the equilibrium against the rho it was built from
+            m = [o.double().cpu().numpy() for o in out]
+            times["rho_roundtrip_max_abs"] = float(np.max(np.abs(m[0] - fields[0])))
+        g.close()
+        res["integer_forms" if mm == "hybrid" else "reference_expressions"] = times
+    del dev, out
+    torch.cuda.empty_cache()
+    return res
 
 
 def time_scheme_steps(torch, n, scheme, math_mode, steps, warmup, fields):
@@ -404,7 +454,7 @@ def main() -> None:
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU-baseline sample length")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-variants", action="store_true")
-    ap.add_argument("--suite", default=None, choices=["mixed"])
+    ap.add_argument("--suite", default=None, choices=["mixed", "fields"])
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.math is None:
@@ -437,6 +487,13 @@ def main() -> None:
             errs = mixed_precision_errors(torch, args.n, 0.52, (1000, 5000, 20000))
             print(json.dumps({"suite": "mixed", "workload": f"shear layer {args.n}^2 BGK tau=0.52 k=80 delta=0.05 "
                               "u0=0.04", "velocity_l2_vs_f64": errs}), flush=True)
+        return
+
+    if args.suite == "fields":
+        if rank == 0:
+            peak = measured_peak_gbs()[0]
+            print(json.dumps({"suite": "fields", **field_kernels_variant(torch, args.n, initial_fields(args.n),
+                                                                          peak)}), flush=True)
         return
 
     n, omega = args.n, 1.0 / args.tau
@@ -592,6 +649,7 @@ def main() -> None:
             var["fp32dev_compensated"]["meets_1e-6"] = max(mp["f32dev/hybrid"].values()) <= 1e-6
         var["fp16dev"]["velocity_l2_vs_f64"] = mp["f16dev/fma"]
         var["fp16dev"]["meets_1e-6"] = max(mp["f16dev/fma"].values()) <= 1e-6
+        var["field_kernels"] = field_kernels_variant(torch, n, fields, peak)
         var["batched_f64"] = batched_variant(torch, "f64", 1000, "hybrid")
         var["batched_f64_fma"] = batched_variant(torch, "f64", 50, both=False)
         var["batched_f32dev"] = batched_variant(torch, "f32dev", 1000)

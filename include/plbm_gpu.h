@@ -151,6 +151,9 @@ int plbm_download(plbm_grid_t *g, double *f_host, int ibuf);
  * (ny,nx) arrays; writes the equilibrium into f(:,:,:,iold) on the device. */
 int plbm_set_pdf_to_equilibrium(plbm_grid_t *g, const double *rho, const double *ux,
                                 const double *uy);
+/* Same from DEVICE (ny,nx) arrays into lattice ibuf, asynchronous. */
+int plbm_equilibrium_device(plbm_grid_t *g, int ibuf, const double *rho, const double *ux,
+                            const double *uy);
 /* grid%streaming() -- lbm_stream (src/periodic_lbm.f90:32-129) or the
  * selected scheme: f(:,:,:,iold) -> f(:,:,:,inew). */
 int plbm_stream(plbm_grid_t *g);
@@ -169,7 +172,14 @@ int plbm_perform_lbm_step(plbm_grid_t *g, int nsteps);
  * iold; every buffer index holds what the Fortran leaves in it. */
 int plbm_perform_triple_step(plbm_grid_t *g, int nsteps);
 /* update_macros -- src/fvm_bardow.F90:343-390: moments of f(:,:,:,inew)
- * into host (ny,nx) arrays.  Any of rho/ux/uy may be NULL. */
+ * into host (ny,nx) arrays.  Any of rho/ux/uy may be NULL.
+ * With PLBM_MATH_HYBRID and PLBM_F64 storage the moments (here and in
+ * plbm_macros_device) and the equilibria (plbm_set_pdf_to_equilibrium,
+ * plbm_equilibrium_device) are integer forms: rho = sum f and u = j / rho
+ * correctly rounded from the exact sums, feq within 0.5 ulp + w_i 2^-58 of
+ * the exact w_i rho (1 + 3 c.u + 4.5 (c.u)^2 - 1.5 u^2); cells outside their
+ * range (f_i < 0 or >= 1, rho >= 8; rho outside (0, 2) or |u| >= 1/4) take
+ * the reference's binary64 expressions.  The other modes evaluate those. */
 int plbm_update_macros(plbm_grid_t *g, double *rho, double *ux, double *uy);
 /* Same moments of lattice ibuf into DEVICE (ny,nx) arrays, asynchronous. */
 int plbm_macros_device(plbm_grid_t *g, int ibuf, double *rho, double *ux, double *uy);

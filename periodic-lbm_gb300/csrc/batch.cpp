@@ -325,7 +325,8 @@ extern "C" int plbm_batch_set_equilibrium(plbm_batch_t* b, int grid, const doubl
   CUDA_TRY(cudaMemcpyAsync(d + n, ux, n * 8, cudaMemcpyHostToDevice, b->stream), "upload ux");
   CUDA_TRY(cudaMemcpyAsync(d + 2 * n, uy, n * 8, cudaMemcpyHostToDevice, b->stream), "upload uy");
   const int st = b->storage == PLBM_F64 ? ST_F64 : ST_F32DEV;
-  CUDA_TRY(equilibrium(st, 0, g.nx, g.ny, g.ld, d, d + n, d + 2 * n, 0, lattice_of(b, grid, current(b)), b->stream),
+  CUDA_TRY(equilibrium(st, 0, g.nx, g.ny, g.ld, d, d + n, d + 2 * n, 0, lattice_of(b, grid, current(b)), b->stream,
+                       b->math == PLBM_MATH_HYBRID),
            "equilibrium kernel");
   CUDA_TRY(cudaStreamSynchronize(b->stream), "equilibrium sync");
   return PLBM_OK;
@@ -417,7 +418,8 @@ extern "C" int plbm_batch_macros(plbm_batch_t* b, int grid, double* rho, double*
   if (int r = ensure_scratch(b, 3 * n)) return r;
   double* d = b->scratch;
   const int st = b->storage == PLBM_F64 ? ST_F64 : ST_F32DEV;
-  CUDA_TRY(macros(st, 0, g.nx, g.ny, g.ld, lattice_of(b, grid, current(b)), d, d + n, d + 2 * n, b->stream),
+  CUDA_TRY(macros(st, 0, g.nx, g.ny, g.ld, lattice_of(b, grid, current(b)), d, d + n, d + 2 * n, b->stream,
+                  b->math == PLBM_MATH_HYBRID),
            "moments kernel");
   if (rho) CUDA_TRY(cudaMemcpyAsync(rho, d, n * 8, cudaMemcpyDeviceToHost, b->stream), "download rho");
   if (ux) CUDA_TRY(cudaMemcpyAsync(ux, d + n, n * 8, cudaMemcpyDeviceToHost, b->stream), "download ux");

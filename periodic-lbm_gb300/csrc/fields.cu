@@ -2,7 +2,11 @@
 // initialisation, storage conversion, vorticity and binary64 reductions.
 // Compiled with --fmad=false: the moments and equilibria then perform the
 // same IEEE operations as update_macros / equilibrium() of the reference.
+// With `exact` (grids in hybrid arithmetic) the binary64 lattices take the
+// integer forms of exact_fields.cuh instead, correctly rounded from the exact
+// moments, cell by cell back to the reference's expressions outside their range.
 #include "plbm_launch.h"
+#include "exact_fields.cuh"
 
 namespace plbm {
 namespace {
@@ -50,7 +54,17 @@ __device__ __forceinline__ void cell_moments(const double (&fs)[9], double& rho,
   }
 }
 
-template <int ST, class L>
+// The reference's moments of a cell outside the exact forms' range, out of
+// line so that the fast path does not carry them.
+template <int ST>
+__device__ __noinline__ void cell_moments_ref(const double* fs, double* out) {
+  double g[9];
+#pragma unroll
+  for (int q = 0; q < 9; q++) g[q] = fs[q];
+  cell_moments<ST>(g, out[0], out[1], out[2]);
+}
+
+template <int ST, class L, bool EXACT>
 __global__ void __launch_bounds__(kBlock) k_macros(const void* __restrict__ f, double* __restrict__ rho,
                                                   double* __restrict__ ux, double* __restrict__ uy, int nx,
                                                   int ny, int ld, int ftiles, int slow0) {
@@ -62,7 +76,17 @@ __global__ void __launch_bounds__(kBlock) k_macros(const void* __restrict__ f, d
 #pragma unroll
   for (int q = 0; q < 9; q++) fs[q] = load_pop<ST>(f, L::off(x, y, q, nx, ny, ld));
   double r, u, v;
-  cell_moments<ST>(fs, r, u, v);
+  if constexpr (EXACT) {
+    bool bad = false;
+    ex::macros_exact<ST == ST_F64SHIFT>(fs, r, u, v, bad);
+    if (bad) {
+      double m[3];
+      cell_moments_ref<ST>(fs, m);
+      r = m[0], u = m[1], v = m[2];
+    }
+  } else {
+    cell_moments<ST>(fs, r, u, v);
+  }
   const size_t o = (size_t)fast + (size_t)nfast * slow;
   if (rho) rho[o] = r;
   if (ux) ux[o] = u;
@@ -105,10 +129,34 @@ __device__ __forceinline__ void eq_shift(double rho, double ux, double uy, doubl
   for (int q = 0; q < 9; q++) feq[q] = feq[q] + w_of(q) * (rho - 1.0);
 }
 
+// The reference's equilibrium of one cell for storage ST (below).
+template <int ST>
+__device__ __forceinline__ void cell_equilibrium(double r, double u, double v, int from_pressure,
+                                                 double (&feq)[9]) {
+  if (ST == ST_F64) {
+    eq_ref(r, u, v, feq);
+  } else if (from_pressure) {
+    eq_shift(1.0 + r / CSQR, u, v, feq);
+  } else {
+    eq_ref(r, u, v, feq);
+#pragma unroll
+    for (int q = 0; q < 9; q++) feq[q] = feq[q] - w_of(q);
+  }
+}
+template <int ST>
+__device__ __noinline__ void cell_equilibrium_ref(double r, double u, double v, int from_pressure, double* out) {
+  double feq[9];
+  cell_equilibrium<ST>(r, u, v, from_pressure, feq);
+#pragma unroll
+  for (int q = 0; q < 9; q++) out[q] = feq[q];
+}
+
 // ST_F64: reference equilibrium of rho.  Shifted storages: from_pressure
 // selects rho = 1 + p/cs^2 (sim/sim.F90:193) and the shifted equilibrium of
-// sim/sim.F90; otherwise the reference equilibrium minus w_i.
-template <int ST, class L>
+// sim/sim.F90; otherwise the reference equilibrium minus w_i.  EXACT (binary64
+// storages only): the integer forms, the reference's expressions for a cell
+// outside their range.
+template <int ST, class L, bool EXACT>
 __global__ void __launch_bounds__(kBlock) k_equilibrium(const double* __restrict__ rho,
                                                        const double* __restrict__ ux,
                                                        const double* __restrict__ uy, int from_pressure,
@@ -120,14 +168,15 @@ __global__ void __launch_bounds__(kBlock) k_equilibrium(const double* __restrict
   const int x = L::x_fast ? fast : slow, y = L::x_fast ? slow : fast;
   const size_t o = (size_t)fast + (size_t)nfast * slow;
   double feq[9];
-  if (ST == ST_F64) {
-    eq_ref(rho[o], ux[o], uy[o], feq);
-  } else if (from_pressure) {
-    eq_shift(1.0 + rho[o] / CSQR, ux[o], uy[o], feq);
+  if constexpr (EXACT) {
+    const double r = rho[o], u = ux[o], v = uy[o];
+    bool bad = false;
+    const int64_t P = (ST == ST_F64SHIFT && from_pressure) ? ex::rho_fixed_from_pressure(r, bad)
+                                                           : ex::rho_fixed(r, bad);
+    ex::equilibrium_exact<ST == ST_F64SHIFT>(P, u, v, feq, bad);
+    if (bad) cell_equilibrium_ref<ST>(r, u, v, from_pressure, feq);
   } else {
-    eq_ref(rho[o], ux[o], uy[o], feq);
-#pragma unroll
-    for (int q = 0; q < 9; q++) feq[q] = feq[q] - w_of(q);
+    cell_equilibrium<ST>(rho[o], ux[o], uy[o], from_pressure, feq);
   }
 #pragma unroll
   for (int q = 0; q < 9; q++) store_pop<ST>(f, L::off(x, y, q, nx, ny, ld), feq[q]);
@@ -234,25 +283,26 @@ __global__ void __launch_bounds__(kBlock) k_energy_error(const void* __restrict_
 }  // namespace
 
 cudaError_t macros(int storage, int layout, int nx, int ny, int ld, const void* f, double* rho, double* ux,
-                   double* uy, cudaStream_t st) {
-  return macros_range(storage, layout, nx, ny, ld, f, rho, ux, uy, 0, layout ? ny : nx, st);
+                   double* uy, cudaStream_t st, bool exact) {
+  return macros_range(storage, layout, nx, ny, ld, f, rho, ux, uy, 0, layout ? ny : nx, st, exact);
 }
 
 cudaError_t macros_range(int storage, int layout, int nx, int ny, int ld, const void* f, double* rho, double* ux,
-                         double* uy, int slow0, int slow1, cudaStream_t st) {
+                         double* uy, int slow0, int slow1, cudaStream_t st, bool exact) {
   const int nfast = layout ? nx : ny, nslow = layout ? ny : nx;
   if (slow0 < 0 || slow1 > nslow || slow0 >= slow1) return cudaErrorInvalidValue;
   const int ft = tiles(nfast);
   const long long blocks = (long long)ft * (slow1 - slow0);
   if (blocks <= 0 || blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
-#define L_(ST, LL) k_macros<ST, LL><<<(unsigned)blocks, kBlock, 0, st>>>(f, rho, ux, uy, nx, ny, ld, ft, slow0)
-#define SW_(LL)                                          \
-  switch (storage) {                                     \
-    case ST_F64: L_(ST_F64, LL); break;                  \
-    case ST_F64SHIFT: L_(ST_F64SHIFT, LL); break;        \
-    case ST_F32DEV: L_(ST_F32DEV, LL); break;            \
-    case ST_F16DEV: L_(ST_F16DEV, LL); break;            \
-    default: return cudaErrorInvalidValue;               \
+#define L_(ST, LL, EX) \
+  k_macros<ST, LL, EX><<<(unsigned)blocks, kBlock, 0, st>>>(f, rho, ux, uy, nx, ny, ld, ft, slow0)
+#define SW_(LL)                                                                \
+  switch (storage) {                                                           \
+    case ST_F64: if (exact) L_(ST_F64, LL, true); else L_(ST_F64, LL, false); break;                  \
+    case ST_F64SHIFT: if (exact) L_(ST_F64SHIFT, LL, true); else L_(ST_F64SHIFT, LL, false); break;   \
+    case ST_F32DEV: L_(ST_F32DEV, LL, false); break;                           \
+    case ST_F16DEV: L_(ST_F16DEV, LL, false); break;                           \
+    default: return cudaErrorInvalidValue;                                     \
   }
   if (layout) { SW_(XFast) } else { SW_(YFast) }
 #undef SW_
@@ -261,26 +311,29 @@ cudaError_t macros_range(int storage, int layout, int nx, int ny, int ld, const 
 }
 
 cudaError_t equilibrium(int storage, int layout, int nx, int ny, int ld, const double* rho, const double* ux,
-                        const double* uy, int from_pressure, void* f, cudaStream_t st) {
-  return equilibrium_range(storage, layout, nx, ny, ld, rho, ux, uy, from_pressure, f, 0, layout ? ny : nx, st);
+                        const double* uy, int from_pressure, void* f, cudaStream_t st, bool exact) {
+  return equilibrium_range(storage, layout, nx, ny, ld, rho, ux, uy, from_pressure, f, 0, layout ? ny : nx, st,
+                           exact);
 }
 
 cudaError_t equilibrium_range(int storage, int layout, int nx, int ny, int ld, const double* rho, const double* ux,
-                              const double* uy, int from_pressure, void* f, int slow0, int slow1, cudaStream_t st) {
+                              const double* uy, int from_pressure, void* f, int slow0, int slow1, cudaStream_t st,
+                              bool exact) {
   const int nfast = layout ? nx : ny, nslow = layout ? ny : nx;
   if (slow0 < 0 || slow1 > nslow || slow0 >= slow1) return cudaErrorInvalidValue;
   const int ft = tiles(nfast);
   const long long blocks = (long long)ft * (slow1 - slow0);
   if (blocks <= 0 || blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
-#define L_(ST, LL) \
-  k_equilibrium<ST, LL><<<(unsigned)blocks, kBlock, 0, st>>>(rho, ux, uy, from_pressure, f, nx, ny, ld, ft, slow0)
-#define SW_(LL)                                          \
-  switch (storage) {                                     \
-    case ST_F64: L_(ST_F64, LL); break;                  \
-    case ST_F64SHIFT: L_(ST_F64SHIFT, LL); break;        \
-    case ST_F32DEV: L_(ST_F32DEV, LL); break;            \
-    case ST_F16DEV: L_(ST_F16DEV, LL); break;            \
-    default: return cudaErrorInvalidValue;               \
+#define L_(ST, LL, EX)                                                                                   \
+  k_equilibrium<ST, LL, EX><<<(unsigned)blocks, kBlock, 0, st>>>(rho, ux, uy, from_pressure, f, nx, ny, ld, ft, \
+                                                                 slow0)
+#define SW_(LL)                                                                \
+  switch (storage) {                                                           \
+    case ST_F64: if (exact) L_(ST_F64, LL, true); else L_(ST_F64, LL, false); break;                  \
+    case ST_F64SHIFT: if (exact) L_(ST_F64SHIFT, LL, true); else L_(ST_F64SHIFT, LL, false); break;   \
+    case ST_F32DEV: L_(ST_F32DEV, LL, false); break;                           \
+    case ST_F16DEV: L_(ST_F16DEV, LL, false); break;                           \
+    default: return cudaErrorInvalidValue;                                     \
   }
   if (layout) { SW_(XFast) } else { SW_(YFast) }
 #undef SW_

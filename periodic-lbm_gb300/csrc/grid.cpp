@@ -382,7 +382,7 @@ extern "C" int plbm_set_pdf_to_equilibrium(plbm_grid_t* g, const double* rho, co
       CUDA_TRY(cudaEventRecord(g->slab_ev[s], g->xfer), "slab event");
       CUDA_TRY(cudaStreamWaitEvent(g->stream, g->slab_ev[s], 0), "slab wait");
       CUDA_TRY(equilibrium_range(internal_storage(g->storage), 0, g->nx, g->ny, g->ld, d, d + n, d + 2 * n, 0,
-                                 lattice(g, g->iold), x0, x1, g->stream),
+                                 lattice(g, g->iold), x0, x1, g->stream, exact_fields(g)),
                "equilibrium kernel");
     }
     CUDA_TRY(cudaStreamSynchronize(g->stream), "equilibrium sync");
@@ -392,7 +392,7 @@ extern "C" int plbm_set_pdf_to_equilibrium(plbm_grid_t* g, const double* rho, co
   CUDA_TRY(cudaMemcpyAsync(d + n, ux, n * 8, cudaMemcpyHostToDevice, g->stream), "upload ux");
   CUDA_TRY(cudaMemcpyAsync(d + 2 * n, uy, n * 8, cudaMemcpyHostToDevice, g->stream), "upload uy");
   CUDA_TRY(equilibrium(internal_storage(g->storage), 0, g->nx, g->ny, g->ld, d, d + n, d + 2 * n, 0,
-                       lattice(g, g->iold), g->stream),
+                       lattice(g, g->iold), g->stream, exact_fields(g)),
            "equilibrium kernel");
   CUDA_TRY(cudaStreamSynchronize(g->stream), "equilibrium sync");
   return ok();
@@ -627,11 +627,24 @@ extern "C" int plbm_perform_triple_step(plbm_grid_t* g, int nsteps) {
   return ok();
 }
 
+extern "C" int plbm_equilibrium_device(plbm_grid_t* g, int ibuf, const double* rho, const double* ux,
+                                       const double* uy) {
+  if (int r = check_grid(g)) return r;
+  if (int r = check_buf(g, ibuf)) return r;
+  if (!rho || !ux || !uy) return fail(PLBM_E_INVALID, "rho, ux and uy must be non-NULL");
+  if (int r = use_device(g)) return r;
+  CUDA_TRY(equilibrium(internal_storage(g->storage), 0, g->nx, g->ny, g->ld, rho, ux, uy, 0, lattice(g, ibuf),
+                       g->stream, exact_fields(g)),
+           "equilibrium kernel");
+  return ok();
+}
+
 extern "C" int plbm_macros_device(plbm_grid_t* g, int ibuf, double* rho, double* ux, double* uy) {
   if (int r = check_grid(g)) return r;
   if (int r = check_buf(g, ibuf)) return r;
   if (int r = use_device(g)) return r;
-  CUDA_TRY(macros(internal_storage(g->storage), 0, g->nx, g->ny, g->ld, lattice(g, ibuf), rho, ux, uy, g->stream),
+  CUDA_TRY(macros(internal_storage(g->storage), 0, g->nx, g->ny, g->ld, lattice(g, ibuf), rho, ux, uy, g->stream,
+                  exact_fields(g)),
            "moments kernel");
   return ok();
 }
@@ -651,7 +664,7 @@ extern "C" int plbm_update_macros(plbm_grid_t* g, double* rho, double* ux, doubl
       int x0, x1;
       slab_bounds(g, s, S, x0, x1);
       CUDA_TRY(macros_range(internal_storage(g->storage), 0, g->nx, g->ny, g->ld, lattice(g, g->inew), d, d + n,
-                            d + 2 * n, x0, x1, g->stream),
+                            d + 2 * n, x0, x1, g->stream, exact_fields(g)),
                "moments kernel");
       CUDA_TRY(cudaEventRecord(g->slab_ev[s], g->stream), "slab event");
       CUDA_TRY(cudaStreamWaitEvent(g->xfer, g->slab_ev[s], 0), "slab wait");
@@ -666,7 +679,7 @@ extern "C" int plbm_update_macros(plbm_grid_t* g, double* rho, double* ux, doubl
     return ok();
   }
   CUDA_TRY(macros(internal_storage(g->storage), 0, g->nx, g->ny, g->ld, lattice(g, g->inew), d, d + n, d + 2 * n,
-                  g->stream),
+                  g->stream, exact_fields(g)),
            "moments kernel");
   if (rho) CUDA_TRY(cudaMemcpyAsync(rho, d, n * 8, cudaMemcpyDeviceToHost, g->stream), "download rho");
   if (ux) CUDA_TRY(cudaMemcpyAsync(ux, d + n, n * 8, cudaMemcpyDeviceToHost, g->stream), "download ux");

@@ -102,4 +102,8 @@ inline int ensure_scratch(plbm_grid_t* g, size_t elems) {
 
 inline int internal_storage(int storage) { return storage; }  // PLBM_F64/F32DEV/F16DEV == ST_*
 
+// Grids in hybrid arithmetic take their moments and equilibria in the exact
+// integer forms too (binary64 storage only).
+inline bool exact_fields(const plbm_grid_t* g) { return g->math == PLBM_MATH_HYBRID && g->storage == PLBM_F64; }
+
 }  // namespace plbm_internal

@@ -198,7 +198,7 @@ extern "C" int plbm_output_npy(plbm_grid_t* g, const char* path) {
   double* d = g->scratch;  // mf(ny,nx,3): rho, ux, uy planes
   // update_macros reads f(:,:,:,inew) (src/fvm_bardow.F90:350-352)
   PLBM_CUDA_TRY(macros(internal_storage(g->storage), 0, g->nx, g->ny, g->ld, lattice(g, g->inew), d, d + n,
-                       d + 2 * n, g->stream),
+                       d + 2 * n, g->stream, exact_fields(g)),
                 "moments kernel");
   std::vector<double> mf(3 * n);
   PLBM_CUDA_TRY(cudaMemcpyAsync(mf.data(), d, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, g->stream),

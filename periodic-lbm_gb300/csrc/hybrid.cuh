@@ -47,7 +47,7 @@ DF_HD double fma_d(double a, double b, double c) {
 #ifdef __CUDA_ARCH__
   return __fma_rn(a, b, c);
 #else
-  return fma(a, b, c);
+  return ::fma(a, b, c);
 #endif
 }
 
@@ -342,7 +342,7 @@ inline double weight_sum_error(const double (&w)[3]) {
 inline double first_moment_error(const double (&w)[3]) {
   double s, e;
   two_sum_d(2.0 * w[1], 4.0 * w[2], s, e);
-  const double p = 3.0 * s, ep = fma(3.0, s, -p);
+  const double p = 3.0 * s, ep = ::fma(3.0, s, -p);
   return (p - 1.0) + (ep + 3.0 * e);
 }
 

@@ -77,24 +77,27 @@ cudaError_t step_pull_dev_hi(int storage, int math, int kind, const Sweep& s, co
 // storage 0 = binary64 f (unshifted), 3 = binary64 shifted, 1/2 = deviation.
 enum { ST_F64 = 0, ST_F32DEV = 1, ST_F16DEV = 2, ST_F64SHIFT = 3 };
 // Moments of one lattice into (fast,slow) arrays; reference order of
-// update_macros (YFast, unshifted) or lbm_macros (shifted).
+// update_macros (YFast, unshifted) or lbm_macros (shifted).  exact (binary64
+// storages 0 and 3): correctly rounded from the exact integer moments instead
+// (exact_fields.cuh), the arithmetic of grids in hybrid mode.
 cudaError_t macros(int storage, int layout, int nx, int ny, int ld, const void* f, double* rho,
-                   double* ux, double* uy, cudaStream_t st);
+                   double* ux, double* uy, cudaStream_t st, bool exact = false);
 // Equilibrium from (fast,slow) rho/ux/uy arrays into a lattice.
 //   storage 0: equilibrium() of src/fvm_bardow.F90:99-126;
 //   storage 3/1/2: shifted equilibrium of sim/sim.F90:353-401 with rho = 1 + p/cs^2
 //   when from_pressure != 0.
+// exact (storages 0 and 3): the integer form of exact_fields.cuh.
 cudaError_t equilibrium(int storage, int layout, int nx, int ny, int ld, const double* rho,
                         const double* ux, const double* uy, int from_pressure, void* f,
-                        cudaStream_t st);
+                        cudaStream_t st, bool exact = false);
 // The same over the slow lines [slow0, slow1) only (x columns of the YFast
 // layout): a slab of the grid, for pipelining with host transfers.  The
 // field pointers still address the whole (fast, slow) arrays.
 cudaError_t macros_range(int storage, int layout, int nx, int ny, int ld, const void* f, double* rho,
-                         double* ux, double* uy, int slow0, int slow1, cudaStream_t st);
+                         double* ux, double* uy, int slow0, int slow1, cudaStream_t st, bool exact = false);
 cudaError_t equilibrium_range(int storage, int layout, int nx, int ny, int ld, const double* rho,
                               const double* ux, const double* uy, int from_pressure, void* f, int slow0,
-                              int slow1, cudaStream_t st);
+                              int slow1, cudaStream_t st, bool exact = false);
 // binary64 f (YFast) <-> deviation storage conversion: h = f - w_i.
 cudaError_t f64_to_dev(int storage, int nx, int ny, int ld, const double* f, void* h, cudaStream_t st);
 cudaError_t dev_to_f64(int storage, int nx, int ny, int ld, const void* h, double* f, cudaStream_t st);

@@ -213,7 +213,7 @@ extern "C" void* c_plbmgpu_init(int nx, int ny, double dt, const double* rho, co
   // lbm_eqinit_fields, sim/sim.F90:181-199
   if (e == cudaSuccess)
     e = equilibrium(st_code(storage), 1, nx, ny, s->ld, s->scratch, s->scratch + n, s->scratch + 2 * n, 1, s->f[0],
-                    s->stream);
+                    s->stream, math == PLBM_MATH_HYBRID);
   // this%grid%f2 = this%grid%f1, sim/sim_slbm.F90:76
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(s->f[1], s->f[0], s->lat_elems * s->elem_bytes, cudaMemcpyDeviceToDevice, s->stream);
@@ -259,7 +259,7 @@ extern "C" void c_plbmgpu_vars(void* p, double* rho, double* u) {
   // lbm_macros of the current state, sim/sim_slbm.F90:112-127
   if (e == cudaSuccess)
     e = macros(st_code(s->storage), 1, s->nx, s->ny, s->ld, s->f[s->cur], s->scratch, s->scratch + n,
-               s->scratch + 2 * n, s->stream);
+               s->scratch + 2 * n, s->stream, s->math == PLBM_MATH_HYBRID);
   if (e == cudaSuccess) e = cudaMemcpyAsync(rho, s->scratch, n * 8, cudaMemcpyDeviceToHost, s->stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(u, s->scratch + n, 2 * n * 8, cudaMemcpyDeviceToHost, s->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);

@@ -95,6 +95,7 @@ SIGNATURES = {
     "plbm_perform_lbm_step": (C.c_int, [_vp, C.c_int]),
     "plbm_update_macros": (C.c_int, [_vp, _vp, _vp, _vp]),
     "plbm_macros_device": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp]),
+    "plbm_equilibrium_device": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp]),
     "plbm_vorticity": (C.c_int, [C.c_int, C.c_int, C.c_int, _vp, _vp, _vp]),
     "plbm_vorticity_device": (C.c_int, [C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp]),
     "plbm_kinetic_energy": (C.c_int, [_vp, C.c_int, _dp]),
