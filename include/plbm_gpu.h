@@ -148,7 +148,11 @@ int plbm_download(plbm_grid_t *g, double *f_host, int ibuf);
 
 /* ---- the hot path ------------------------------------------------------- */
 /* set_pdf_to_equilibrium -- src/fvm_bardow.F90:272-305.  rho, ux, uy are host
- * (ny,nx) arrays; writes the equilibrium into f(:,:,:,iold) on the device. */
+ * (ny,nx) arrays; writes the equilibrium into f(:,:,:,iold) on the device.
+ * Page-locked (pinned, mapped) host arrays are read in place by the kernel;
+ * pageable ones are staged through device memory (in x-column slabs that
+ * overlap copies and kernels on grids of 2^22 cells or more).  The same holds
+ * for the outputs of plbm_update_macros. */
 int plbm_set_pdf_to_equilibrium(plbm_grid_t *g, const double *rho, const double *ux,
                                 const double *uy);
 /* Same from DEVICE (ny,nx) arrays into lattice ibuf, asynchronous. */

@@ -336,6 +336,20 @@ namespace {
 // copy of one slab overlaps the kernel of the previous one
 // (set_pdf_to_equilibrium: copy then equilibrium; update_macros: moments
 // then copy).  About 96 MB of fields per slab, at most kMaxSlabs.
+// Device address of a host array that is page-locked and mapped (cudaHostAlloc
+// / cudaMallocHost / cudaHostRegister under unified addressing), else NULL
+// (pageable memory, or NULL).  The field kernels then read or write the host
+// array directly over the host link: no staging buffer, and no copy engine.
+const void* mapped_host(const void* p) {
+  if (!p) return nullptr;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 int slab_count(const plbm_grid_t* g) {
   const size_t n = (size_t)g->nx * g->ny;
   if (n < ((size_t)1 << 22) || g->nx < 4) return 1;
@@ -362,6 +376,15 @@ extern "C" int plbm_set_pdf_to_equilibrium(plbm_grid_t* g, const double* rho, co
   if (int r = check_grid(g)) return r;
   if (!rho || !ux || !uy) return fail(PLBM_E_INVALID, "rho, ux and uy must be non-NULL");
   if (int r = use_device(g)) return r;
+  const void *mr = mapped_host(rho), *mu = mapped_host(ux), *mv = mapped_host(uy);
+  if (mr && mu && mv) {  // page-locked host fields: the kernel reads them in place
+    CUDA_TRY(equilibrium(internal_storage(g->storage), 0, g->nx, g->ny, g->ld, static_cast<const double*>(mr),
+                         static_cast<const double*>(mu), static_cast<const double*>(mv), 0, lattice(g, g->iold),
+                         g->stream, exact_fields(g)),
+             "equilibrium kernel");
+    CUDA_TRY(cudaStreamSynchronize(g->stream), "equilibrium sync");
+    return ok();
+  }
   const size_t n = (size_t)g->nx * g->ny;
   if (int r = ensure_scratch(g, 3 * n)) return r;
   double* d = g->scratch;
@@ -652,6 +675,19 @@ extern "C" int plbm_macros_device(plbm_grid_t* g, int ibuf, double* rho, double*
 extern "C" int plbm_update_macros(plbm_grid_t* g, double* rho, double* ux, double* uy) {
   if (int r = check_grid(g)) return r;
   if (int r = use_device(g)) return r;
+  {
+    // page-locked host outputs (every one given): the kernel writes them in place
+    void *mr = const_cast<void*>(mapped_host(rho)), *mu = const_cast<void*>(mapped_host(ux)),
+         *mv = const_cast<void*>(mapped_host(uy));
+    if ((rho || ux || uy) && (!rho || mr) && (!ux || mu) && (!uy || mv)) {
+      CUDA_TRY(macros(internal_storage(g->storage), 0, g->nx, g->ny, g->ld, lattice(g, g->inew),
+                      static_cast<double*>(mr), static_cast<double*>(mu), static_cast<double*>(mv), g->stream,
+                      exact_fields(g)),
+               "moments kernel");
+      CUDA_TRY(cudaStreamSynchronize(g->stream), "update_macros sync");
+      return ok();
+    }
+  }
   const size_t n = (size_t)g->nx * g->ny;
   if (int r = ensure_scratch(g, 3 * n)) return r;
   double* d = g->scratch;
