@@ -341,6 +341,31 @@ cudaError_t equilibrium_range(int storage, int layout, int nx, int ny, int ld, c
   return cudaGetLastError();
 }
 
+namespace {
+__global__ void __launch_bounds__(kBlock) k_copy2(const double2* __restrict__ s, double2* __restrict__ d, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    d[i] = s[i];
+}
+__global__ void __launch_bounds__(kBlock) k_copy1(const double* __restrict__ s, double* __restrict__ d, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    d[i] = s[i];
+}
+}  // namespace
+
+cudaError_t copy_doubles(const double* src, double* dst, size_t n, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  int dev = 0, sms = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  const unsigned blocks = (unsigned)(sms > 0 ? sms * 8 : 1024);
+  if ((((uintptr_t)src | (uintptr_t)dst) & 15u) == 0 && n % 2 == 0)
+    k_copy2<<<blocks, kBlock, 0, st>>>(reinterpret_cast<const double2*>(src), reinterpret_cast<double2*>(dst), n / 2);
+  else
+    k_copy1<<<blocks, kBlock, 0, st>>>(src, dst, n);
+  return cudaGetLastError();
+}
+
 cudaError_t f64_to_dev(int storage, int nx, int ny, int ld, const double* f, void* h, cudaStream_t st) {
   const int ft = tiles(ny);
   const long long blocks = (long long)ft * nx;

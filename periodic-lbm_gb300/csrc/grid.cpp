@@ -285,12 +285,39 @@ extern "C" int plbm_set_math(plbm_grid_t* g, int math) {
 }
 
 // ---------------------------------------------------------------------------
+namespace {
+// Device address of a host array that is page-locked and mapped (cudaHostAlloc
+// / cudaMallocHost / cudaHostRegister under unified addressing), else NULL
+// (pageable memory, or NULL).  The field kernels then read or write the host
+// array directly over the host link: no staging buffer, and no copy engine.
+const void* mapped_host(const void* p) {
+  if (!p) return nullptr;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+}  // namespace
+
 extern "C" int plbm_upload(plbm_grid_t* g, const double* f_host, int ibuf) {
   if (int r = check_grid(g)) return r;
   if (int r = check_buf(g, ibuf)) return r;
   if (!f_host) return fail(PLBM_E_INVALID, "f_host is NULL");
   if (int r = use_device(g)) return r;
   const size_t bytes64 = g->lat_elems * sizeof(double);
+  if (const void* m = mapped_host(f_host)) {  // page-locked: read in place by the kernel
+    const double* src = static_cast<const double*>(m);
+    if (g->storage == PLBM_F64)
+      CUDA_TRY(copy_doubles(src, static_cast<double*>(lattice(g, ibuf)), g->lat_elems, g->stream), "upload");
+    else
+      CUDA_TRY(f64_to_dev(internal_storage(g->storage), g->nx, g->ny, g->ld, src, lattice(g, ibuf), g->stream),
+               "upload (deviation conversion)");
+    CUDA_TRY(cudaStreamSynchronize(g->stream), "upload sync");
+    return ok();
+  }
   if (g->storage == PLBM_F64) {
     CUDA_TRY(cudaMemcpyAsync(lattice(g, ibuf), f_host, bytes64, cudaMemcpyHostToDevice, g->stream), "upload");
     CUDA_TRY(cudaStreamSynchronize(g->stream), "upload sync");
@@ -312,6 +339,14 @@ extern "C" int plbm_download(plbm_grid_t* g, double* f_host, int ibuf) {
   if (!f_host) return fail(PLBM_E_INVALID, "f_host is NULL");
   if (int r = use_device(g)) return r;
   const size_t bytes64 = g->lat_elems * sizeof(double);
+  const void* m = g->storage == PLBM_F64 ? mapped_host(f_host) : nullptr;
+  if (m) {  // page-locked: written in place by the kernel
+    CUDA_TRY(copy_doubles(static_cast<const double*>(lattice(g, ibuf)), static_cast<double*>(const_cast<void*>(m)),
+                          g->lat_elems, g->stream),
+             "download");
+    CUDA_TRY(cudaStreamSynchronize(g->stream), "download sync");
+    return ok();
+  }
   if (g->storage == PLBM_F64) {
     CUDA_TRY(cudaMemcpyAsync(f_host, lattice(g, ibuf), bytes64, cudaMemcpyDeviceToHost, g->stream), "download");
     CUDA_TRY(cudaStreamSynchronize(g->stream), "download sync");
@@ -336,20 +371,6 @@ namespace {
 // copy of one slab overlaps the kernel of the previous one
 // (set_pdf_to_equilibrium: copy then equilibrium; update_macros: moments
 // then copy).  About 96 MB of fields per slab, at most kMaxSlabs.
-// Device address of a host array that is page-locked and mapped (cudaHostAlloc
-// / cudaMallocHost / cudaHostRegister under unified addressing), else NULL
-// (pageable memory, or NULL).  The field kernels then read or write the host
-// array directly over the host link: no staging buffer, and no copy engine.
-const void* mapped_host(const void* p) {
-  if (!p) return nullptr;
-  cudaPointerAttributes a;
-  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
-    cudaGetLastError();
-    return nullptr;
-  }
-  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
-}
-
 int slab_count(const plbm_grid_t* g) {
   const size_t n = (size_t)g->nx * g->ny;
   if (n < ((size_t)1 << 22) || g->nx < 4) return 1;

@@ -98,6 +98,9 @@ cudaError_t macros_range(int storage, int layout, int nx, int ny, int ld, const 
 cudaError_t equilibrium_range(int storage, int layout, int nx, int ny, int ld, const double* rho,
                               const double* ux, const double* uy, int from_pressure, void* f, int slow0,
                               int slow1, cudaStream_t st, bool exact = false);
+// n doubles from src to dst (device addresses; either may be a mapped host
+// array), by a kernel: 16-byte accesses when both are 16-byte aligned.
+cudaError_t copy_doubles(const double* src, double* dst, size_t n, cudaStream_t st);
 // binary64 f (YFast) <-> deviation storage conversion: h = f - w_i.
 cudaError_t f64_to_dev(int storage, int nx, int ny, int ld, const double* f, void* h, cudaStream_t st);
 cudaError_t dev_to_f64(int storage, int nx, int ny, int ld, const void* h, double* f, cudaStream_t st);

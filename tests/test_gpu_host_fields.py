@@ -71,3 +71,28 @@ def test_mixed_and_null_outputs(gpu_lib):
     _lib.check(lib.plbm_update_macros(g.handle, None, pu.ctypes.data, None))
     assert np.array_equal(pu, want[1])
     g.close()
+
+
+@pytest.mark.parametrize("storage", ["f64", "f32dev", "f16dev"])
+def test_pinned_lattice_upload_and_download(gpu_lib, storage):
+    """plbm_upload / plbm_download with a page-locked lattice: copied (and for
+    deviation storage converted) by kernels reading or writing it in place;
+    the same lattices as through the staged path."""
+    from plbm import LatticeGrid, _lib
+    from oracle import oracle as O
+    lib = _lib.load()
+    nx, ny = 48, 30
+    f = O.set_pdf_to_equilibrium(*fields(nx, ny, 9))
+    g = LatticeGrid(nx, ny, collision="bgk", storage=storage)
+    fp = pinned(f.shape)
+    fp[...] = f
+    _lib.check(lib.plbm_upload(g.handle, fp.ctypes.data, 1))
+    g.upload(f, 2)
+    a = g.download(1)
+    b = g.download(2)
+    assert np.array_equal(a, b)
+    dp = pinned(f.shape)
+    dp[...] = np.nan
+    _lib.check(lib.plbm_download(g.handle, dp.ctypes.data, 1))
+    assert np.array_equal(dp, a)  # deviation storage downloads stay staged
+    g.close()
