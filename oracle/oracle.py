@@ -3,7 +3,9 @@
 TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() and
 by bench.py's CPU-baseline leg, as the checker.  The product never imports it.
 
-Parity status: unpinned against the reference binary (see plbm_oracle.h).
+Parity status: pinned to the reference binary's printed Taylor-Green errors
+for the finite-difference Bardow streaming with BGK; unpinned for TRT, RR,
+the improved BGK and lbm_stream (see plbm_oracle.h).
 
 Array conventions follow the Fortran memory order:
   lattice f(ld,nx,0:8)        -> C-order numpy array (9, nx, ld)

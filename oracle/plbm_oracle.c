@@ -4,8 +4,11 @@
  * TEST INFRASTRUCTURE ONLY: the checker for the CUDA path and the timed CPU
  * baseline.  Nothing in the product links, loads or calls this file.
  *
- * Parity status: UNPINNED against the reference binary (no Fortran compiler on
- * either machine; the reference holds no golden vectors for this path).  Each
+ * Parity status: pinned to the reference binary's printed Taylor-Green errors
+ * for the finite-difference Bardow streaming with BGK (graphs/fvm_bardow_64.txt;
+ * tests/test_reference_bardow64.py); unpinned for TRT, RR, the improved BGK and
+ * lbm_stream (no Fortran compiler on either machine; the reference holds no
+ * other output for them).  See plbm_oracle.h.  Each
  * routine cites the Fortran it restates and keeps the Fortran evaluation
  * order: Fortran evaluates a+b+c as (a+b)+c and a*b*c as (a*b)*c and never
  * breaks parentheses, so every expression below is written with the same

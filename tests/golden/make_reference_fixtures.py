@@ -14,6 +14,12 @@ initial fields, the state after the run, the simulated time and the error
 norms the reference's study computes (norm1, norm2, the plugin's my_norm of
 u_x, norm2x, norm2y) in tests/golden/reference_plugin.npz.  The GPU plugin
 tests start libplbmgpu.so from the same fields and compare with these.
+
+It also copies the reference's recorded Taylor-Green temporal-error curve
+(graphs/fvm_bardow_64.txt: dt/tau and the velocity L2 error of its driver
+with the finite-difference Bardow streaming and BGK on a 64 x 64 grid, 21
+points) into tests/golden/reference_bardow64.npz as the expected values of
+tests/test_reference_bardow64.py and tests/test_gpu_reference_bardow64.py.
 """
 from __future__ import annotations
 
@@ -26,6 +32,7 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 ROOT = HERE.parents[1]
 OUT = HERE / "reference_plugin.npz"
+OUT_BARDOW = HERE / "reference_bardow64.npz"
 
 
 def cases():
@@ -74,6 +81,10 @@ def main() -> None:
     z = make(RP.load_cases(), str(ROOT / "oracle" / "liboracleplugin.so"))
     np.savez_compressed(OUT, **z)
     print(f"wrote {OUT} ({len(z)} arrays)")
+    import reference_tgv as RT
+    pts = RT.read_reference_file(RP.reference_dir())
+    np.savez_compressed(OUT_BARDOW, dt_over_tau_l2=pts)
+    print(f"wrote {OUT_BARDOW} ({pts.shape[0]} points)")
 
 
 if __name__ == "__main__":
