@@ -13,7 +13,7 @@ straight binary64 kernel is measured beside it ("variants.fp64_native").
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                     [--n 8192] [--kind bgk|trt|rr] [--storage f64|f32dev|f16dev]
                     [--math fma|strict|hybrid] [--no-variants] [--no-cpu-baseline]
-                    [--suite mixed|fields]
+                    [--suite mixed|fields|adjoint]
 
 Prints one JSON line (rank 0).  --impl reference times the reference's
 algorithm on the host cores instead: the C restatement of the Fortran
@@ -22,7 +22,9 @@ algorithm on the host cores instead: the C restatement of the Fortran
 velocity L2 error of binary32/binary16 deviation storage against binary64 at
 steps 1000/5000/20000) and prints its own JSON line; --suite fields times the
 two field kernels around the job (equilibrium, moments) on device-resident
-fields, integer forms and reference expressions ("variants.field_kernels").
+fields, integer forms and reference expressions ("variants.field_kernels");
+--suite adjoint times the config-5 adjoint alone (1024^2, T = 2000, K = 45,
+binary32 storage; "variants.adjoint_f32dev").
 """
 from __future__ import annotations
 
@@ -454,7 +456,7 @@ def main() -> None:
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU-baseline sample length")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-variants", action="store_true")
-    ap.add_argument("--suite", default=None, choices=["mixed", "fields"])
+    ap.add_argument("--suite", default=None, choices=["mixed", "fields", "adjoint"])
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.math is None:
@@ -487,6 +489,11 @@ def main() -> None:
             errs = mixed_precision_errors(torch, args.n, 0.52, (1000, 5000, 20000))
             print(json.dumps({"suite": "mixed", "workload": f"shear layer {args.n}^2 BGK tau=0.52 k=80 delta=0.05 "
                               "u0=0.04", "velocity_l2_vs_f64": errs}), flush=True)
+        return
+
+    if args.suite == "adjoint":
+        if rank == 0:
+            print(json.dumps({"suite": "adjoint", **adjoint_variant(torch, "f32dev")}), flush=True)
         return
 
     if args.suite == "fields":

@@ -335,7 +335,10 @@ int plbm_batch_download(plbm_batch_t *b, int grid, double *f);
  * No counterpart in the reference.  Hand-written reverse step: the Jacobian
  * transpose of the BGK collision applied matrix-free, then streaming
  * transposed (a push along -c_q).  Memory is bounded by checkpointing every
- * checkpoint_every steps and recomputing each segment; dL/domega is
+ * checkpoint_every (K) steps and recomputing each segment: ceil(T/K) + 2K + 4
+ * lattices, the recomputation of the next segment running on a second stream
+ * of the handle beside the reverse steps of the current one (ordered by
+ * events; the call's work still ends on the caller's stream).  dL/domega is
  * accumulated in binary64.  storage PLBM_F64 (binary64 arithmetic) or
  * PLBM_F32DEV (binary32 storage and per-cell arithmetic).
  * All field pointers are DEVICE arrays of 2*nx*ny doubles: component a of

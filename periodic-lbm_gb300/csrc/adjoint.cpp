@@ -2,11 +2,17 @@
 // reverse sweep with recomputation (sqrt(T) memory), see adjoint.cu.
 //
 // Checkpoints hold f_n for n = 0, K, 2K, ... (K = checkpoint_every).  The
-// reverse sweep walks the segments [kK, min(kK+K, T)) from the last: it
-// recomputes the segment's states from checkpoint k into a K-lattice buffer,
-// then applies the reverse steps n = end-1 .. kK.  Device memory:
-// (ceil(T/K) + K + 4) lattices.  Each forward step is computed twice in all
-// (forward pass + recomputation).
+// reverse sweep walks the segments [kK, min(kK+K, T)) from the last: the
+// segment's states are recomputed from checkpoint k into a K-lattice buffer,
+// then the reverse steps n = end-1 .. kK run.  Two segment buffers alternate:
+// while the reverse steps of segment k run on the caller's stream, the
+// recomputation of segment k-1 runs on a second stream into the other buffer
+// (events order each recomputation after the reverse sweep that last read
+// its buffer, and each reverse sweep after its recomputation).  The two
+// kernels' streams share the SMs and HBM: neither fills the GPU alone at
+// 1024^2 (tails of 4096-CTA launches, load latency).  Device memory:
+// (ceil(T/K) + 2K + 4) lattices with more than one segment.  Each forward
+// step is computed twice in all (forward pass + recomputation).
 #include <cuda_runtime.h>
 #include <string.h>
 #include <vector>
@@ -34,7 +40,7 @@ struct plbm_adjoint {
   int nx, ny, ld, storage, nsteps, K, nck, device;
   size_t lat_bytes;
   char* ck = nullptr;    // nck lattices
-  char* seg = nullptr;   // K lattices
+  char* seg = nullptr;   // nseg x K lattices (nseg = 2 with more than one segment)
   char* work = nullptr;  // 2 lattices
   char* lam = nullptr;   // 2 lattices
   double* u0 = nullptr;  // 2*nx*ny
@@ -43,7 +49,10 @@ struct plbm_adjoint {
   double omega = 1.0;
   const void* fT = nullptr;
   int have_forward = 0;
+  int nseg = 1;
   cudaStream_t own = nullptr, stream = nullptr;
+  cudaStream_t side = nullptr;          // recomputation stream
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_rec[2] = {nullptr, nullptr}, ev_rev[2] = {nullptr, nullptr};
 };
 
 namespace {
@@ -52,8 +61,9 @@ int pad16(int n) { return n % 16 ? n + (16 - n % 16) : n; }
 
 void* lat(char* base, const plbm_adjoint_t* a, int i) { return base + (size_t)i * a->lat_bytes; }
 
-cudaError_t fwd_step(const plbm_adjoint_t* a, const void* src, void* dst, const CollParams& p) {
-  Sweep s{a->nx, a->ny, a->ld, src, dst, a->stream};
+cudaError_t fwd_step(const plbm_adjoint_t* a, const void* src, void* dst, const CollParams& p,
+                     cudaStream_t stream) {
+  Sweep s{a->nx, a->ny, a->ld, src, dst, stream};
   if (a->storage == PLBM_F64) return fma::step_pull_f64(K_BGK, s, p);
   return step_pull_dev(ST_F32DEV, K_BGK, s, p);
 }
@@ -98,18 +108,22 @@ extern "C" int plbm_adjoint_create(int nx, int ny, int storage, int nsteps, int 
   cudaGetDevice(&a->device);
   a->lat_bytes = (size_t)a->ld * nx * 9 * (storage == PLBM_F64 ? 8 : 4);
   a->nblocks = adjoint_blocks(nx, ny);
+  a->nseg = a->nck > 1 ? 2 : 1;
   cudaError_t e = cudaMalloc(&a->ck, a->lat_bytes * a->nck);
-  if (e == cudaSuccess) e = cudaMalloc(&a->seg, a->lat_bytes * a->K);
+  if (e == cudaSuccess) e = cudaMalloc(&a->seg, a->lat_bytes * a->K * a->nseg);
   if (e == cudaSuccess) e = cudaMalloc(&a->work, a->lat_bytes * 2);
   if (e == cudaSuccess) e = cudaMalloc(&a->lam, a->lat_bytes * 2);
   if (e == cudaSuccess) e = cudaMalloc(&a->u0, sizeof(double) * 2 * (size_t)nx * ny);
   if (e == cudaSuccess) e = cudaMalloc(&a->dom, sizeof(double) * a->nblocks);
   // padding rows are never written by the kernels: give them a defined value
   if (e == cudaSuccess) e = cudaMemset(a->ck, 0, a->lat_bytes * a->nck);
-  if (e == cudaSuccess) e = cudaMemset(a->seg, 0, a->lat_bytes * a->K);
+  if (e == cudaSuccess) e = cudaMemset(a->seg, 0, a->lat_bytes * a->K * a->nseg);
   if (e == cudaSuccess) e = cudaMemset(a->work, 0, a->lat_bytes * 2);
   if (e == cudaSuccess) e = cudaMemset(a->lam, 0, a->lat_bytes * 2);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&a->own, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&a->side, cudaStreamNonBlocking);
+  cudaEvent_t* evs[6] = {&a->ev_fork, &a->ev_join, &a->ev_rec[0], &a->ev_rec[1], &a->ev_rev[0], &a->ev_rev[1]};
+  for (int i = 0; i < 6 && e == cudaSuccess; i++) e = cudaEventCreateWithFlags(evs[i], cudaEventDisableTiming);
   if (e != cudaSuccess) {
     plbm_adjoint_destroy(a);
     return cuda_fail(e, "adjoint allocation");
@@ -123,6 +137,7 @@ extern "C" int plbm_adjoint_destroy(plbm_adjoint_t* a) {
   if (!a) return PLBM_OK;
   cudaSetDevice(a->device);
   if (a->stream) cudaStreamSynchronize(a->stream);
+  if (a->side) cudaStreamSynchronize(a->side);
   cudaFree(a->ck);
   cudaFree(a->seg);
   cudaFree(a->work);
@@ -130,6 +145,10 @@ extern "C" int plbm_adjoint_destroy(plbm_adjoint_t* a) {
   cudaFree(a->u0);
   cudaFree(a->dom);
   if (a->own) cudaStreamDestroy(a->own);
+  if (a->side) cudaStreamDestroy(a->side);
+  cudaEvent_t evs[6] = {a->ev_fork, a->ev_join, a->ev_rec[0], a->ev_rec[1], a->ev_rev[0], a->ev_rev[1]};
+  for (cudaEvent_t ev : evs)
+    if (ev) cudaEventDestroy(ev);
   delete a;
   return PLBM_OK;
 }
@@ -142,7 +161,8 @@ extern "C" int plbm_adjoint_set_stream(plbm_adjoint_t* a, void* stream) {
 
 extern "C" int plbm_adjoint_memory(const plbm_adjoint_t* a, size_t* bytes) {
   if (!a || !bytes) return fail(PLBM_E_INVALID, "NULL argument");
-  *bytes = a->lat_bytes * ((size_t)a->nck + a->K + 4) + sizeof(double) * (2 * (size_t)a->nx * a->ny + a->nblocks);
+  *bytes = a->lat_bytes * ((size_t)a->nck + (size_t)a->K * a->nseg + 4) +
+           sizeof(double) * (2 * (size_t)a->nx * a->ny + a->nblocks);
   return PLBM_OK;
 }
 
@@ -163,7 +183,7 @@ extern "C" int plbm_adjoint_forward(plbm_adjoint_t* a, const double* u0, double 
   for (int n = 0; n < a->nsteps; n++) {
     void* dst = lat(a->work, a, tog);
     tog ^= 1;
-    CUDA_TRY(fwd_step(a, cur, dst, p), "forward step");
+    CUDA_TRY(fwd_step(a, cur, dst, p, a->stream), "forward step");
     cur = dst;
     if ((n + 1) % a->K == 0 && (n + 1) < a->nsteps)
       CUDA_TRY(cudaMemcpyAsync(lat(a->ck, a, (n + 1) / a->K), cur, a->lat_bytes, cudaMemcpyDeviceToDevice, a->stream),
@@ -192,25 +212,48 @@ extern "C" int plbm_adjoint_backward(plbm_adjoint_t* a, const double* grad_uT, d
   CUDA_TRY(adjoint_launch(st(a), 1, L), "lambda_T kernel");
   CUDA_TRY(cudaMemsetAsync(a->dom, 0, sizeof(double) * a->nblocks, a->stream), "clear domega");
   const CollParams p = plbm_make_params(a->omega, 0.25);
+  // segment k's states live in buffer k % nseg
+  auto seg_lat = [a](int k, int i) { return lat(a->seg, a, (k % a->nseg) * a->K + i); };
+  auto seg_end = [a](int k) { return k * a->K + a->K < a->nsteps ? k * a->K + a->K : a->nsteps; };
+  // recompute f_{n0+1} .. f_{n1-1} of segment k into its buffer, on the side stream
+  auto recompute = [&](int k) -> int {
+    const int n0 = k * a->K, n1 = seg_end(k);
+    for (int i = 1; i < n1 - n0; i++) {
+      const void* src = i == 1 ? lat(a->ck, a, k) : seg_lat(k, i - 1);
+      CUDA_TRY(fwd_step(a, src, seg_lat(k, i), p, a->side), "recompute step");
+    }
+    CUDA_TRY(cudaEventRecord(a->ev_rec[k & 1], a->side), "record recomputation");
+    return PLBM_OK;
+  };
+  // the side stream starts after everything queued on the caller's stream
+  CUDA_TRY(cudaEventRecord(a->ev_fork, a->stream), "record fork");
+  CUDA_TRY(cudaStreamWaitEvent(a->side, a->ev_fork, 0), "fork");
+  int rc = recompute(a->nck - 1);
+  if (rc != PLBM_OK) return rc;
   int li = 0;
   for (int k = a->nck - 1; k >= 0; k--) {
-    const int n0 = k * a->K;
-    const int n1 = n0 + a->K < a->nsteps ? n0 + a->K : a->nsteps;
-    // recompute f_{n0+1} .. f_{n1-1} into seg[1..]
-    for (int i = 1; i < n1 - n0; i++) {
-      const void* src = i == 1 ? lat(a->ck, a, k) : lat(a->seg, a, i - 1);
-      CUDA_TRY(fwd_step(a, src, lat(a->seg, a, i), p), "recompute step");
+    if (k >= 1) {
+      // segment k-1 reuses the buffer of segment k+1: after its reverse sweep
+      if (k + 1 < a->nck) CUDA_TRY(cudaStreamWaitEvent(a->side, a->ev_rev[(k + 1) & 1], 0), "wait reverse sweep");
+      rc = recompute(k - 1);
+      if (rc != PLBM_OK) return rc;
     }
-    for (int n = n1 - 1; n >= n0; n--) {
+    CUDA_TRY(cudaStreamWaitEvent(a->stream, a->ev_rec[k & 1], 0), "wait recomputation");
+    const int n0 = k * a->K;
+    for (int n = seg_end(k) - 1; n >= n0; n--) {
       L = base_launch(a);
-      L.f = n == n0 ? lat(a->ck, a, k) : lat(a->seg, a, n - n0);
+      L.f = n == n0 ? lat(a->ck, a, k) : seg_lat(k, n - n0);
       L.lam_in = lat(a->lam, a, li);
       L.lam_out = lat(a->lam, a, 1 - li);
       L.dom = a->dom;
       CUDA_TRY(adjoint_launch(st(a), 2, L), "reverse step");
       li = 1 - li;
     }
+    CUDA_TRY(cudaEventRecord(a->ev_rev[k & 1], a->stream), "record reverse sweep");
   }
+  // join: nothing of the side stream outlives the call's work on the caller's stream
+  CUDA_TRY(cudaEventRecord(a->ev_join, a->side), "record join");
+  CUDA_TRY(cudaStreamWaitEvent(a->stream, a->ev_join, 0), "join");
   if (grad_u0) {
     L = base_launch(a);
     L.lam_in = lat(a->lam, a, li);
