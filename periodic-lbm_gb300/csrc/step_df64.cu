@@ -121,10 +121,9 @@ __device__ __noinline__ void hybrid_fallback_cell(const double* __restrict__ src
   g_hybrid_range_flag = 1;
 }
 
-// Resident CTAs per SM the hybrid kernels are compiled for: TRT at 5
-// (register cap 65536 / (256 x 5) = 48; measured best at 8192^2), BGK (bgk_fma)
-// at 4 and RR (rr_fma) at 3, the caps under which they need no spills (64 and
-// 80 registers).
+// Resident CTAs per SM the hybrid kernels are compiled for: BGK (bgk_fma) and
+// TRT (trt_fma) at 4, RR (rr_fma) at 3 (register caps 64 and 80).  Capped at
+// 48 registers for 5 CTAs the BGK kernel spills and runs 2 % slower at 8192^2.
 constexpr int hybrid_min_blocks(int kind) { return kind == K_RR ? 3 : 4; }
 
 // I: index type of the lattice offsets; 32-bit when the whole lattice has
