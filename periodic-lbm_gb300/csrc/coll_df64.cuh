@@ -109,6 +109,16 @@ DF_HD float relax(float h, float d, float om_hi, float om_lo) {
   return t + c;
 }
 
+// The update of a pair (q, qbar = -q): heq = a +- b with a = w (drho + rho nl_q)
+// (nl_q = 4.5 (c_q.u)^2 - 1.5 u^2) and b = 3 w c_q.j.  With the pair's exact
+// sum S = h_q + h_qbar and difference D = h_q - h_qbar (the error-free sums
+// the moments are built from),
+//   heq_q - h_q = (a - S/2) + (b - D/2),  heq_qbar - h_qbar = (a - S/2) - (b - D/2):
+// a - S/2 and b - D/2 are the symmetric and antisymmetric non-equilibrium
+// parts, small against a and b, so their high parts subtract exactly (the
+// operands are within a factor two; the FMA with -1/2 forms S/2 exactly) and
+// their low parts add in binary32.  This replaces the double-float sums
+// a + b, a - b of the two equilibria and 12 binary32 operations per pair.
 DF_HD void bgk_dev_comp(float (&h)[9], const DevParams& p) {
   // exact pairwise sums and differences of the stored values
   const df64 s13 = two_sum(h[1], h[3]), s24 = two_sum(h[2], h[4]);
@@ -126,28 +136,29 @@ DF_HD void bgk_dev_comp(float (&h)[9], const DevParams& p) {
   const float rho = 1.0f + dr;
   const float u2 = 1.5f * (ux * ux + uy * uy);
   // h' = h + omega (heq - h), heq = w (drho + rho (4.5 (c.u)^2 - 1.5 u^2)) + 3 w c.j.
-  // Only heq needs more than binary32: it is formed in double-float, the
-  // nonlinear term (binary32) joining the exact drho before the product with
-  // w (binary32 weights in that product biased the relaxation rate by ~1e-8);
-  // heq - h is a small difference of nearby values and takes binary32; relax()
-  // adds omega (heq - h) with one rounding, to the storage format.
+  // The equilibrium's O(h) part is formed in double-float, the nonlinear term
+  // (binary32) joining the exact drho before the product with w (binary32
+  // weights in that product biased the relaxation rate by ~1e-8); heq - h is a
+  // small difference of nearby values and takes binary32; relax() adds
+  // omega (heq - h) with one rounding, to the storage format.
   {
     const df64 e = mul_lazy(p.w[0], add_lazy(drho, make(rho * -u2, 0.0f)));
     h[0] = relax(h[0], (e.hi - h[0]) + e.lo, p.om_hi, p.om_lo);
   }
-#define PLBM_COMP_PAIR(QP, QM, CUF, CJ, WI)                                              \
-  {                                                                                      \
-    const float cu = (CUF);                                                              \
-    const df64 a = mul_lazy(p.w[WI], add_lazy(drho, make(rho * fmaf_(4.5f * cu, cu, -u2), 0.0f))); \
-    const df64 b = mul_lazy(p.w3[WI], CJ);                                               \
-    const df64 ep = add_lazy(a, b), em = add_lazy(a, neg(b));                            \
-    h[QP] = relax(h[QP], (ep.hi - h[QP]) + ep.lo, p.om_hi, p.om_lo);                     \
-    h[QM] = relax(h[QM], (em.hi - h[QM]) + em.lo, p.om_hi, p.om_lo);                     \
+#define PLBM_COMP_PAIR(QP, QM, CUF, CJ, S, D, WI)                                                       \
+  {                                                                                                    \
+    const float cu = (CUF);                                                                            \
+    const df64 a = mul_lazy(p.w[WI], add_lazy(drho, make(rho * fmaf_(4.5f * cu, cu, -u2), 0.0f)));    \
+    const df64 b = mul_lazy(p.w3[WI], CJ);                                                             \
+    const float sym = fmaf_(-0.5f, S.hi, a.hi) + fmaf_(-0.5f, S.lo, a.lo);                             \
+    const float asym = fmaf_(-0.5f, D.hi, b.hi) + fmaf_(-0.5f, D.lo, b.lo);                            \
+    h[QP] = relax(h[QP], sym + asym, p.om_hi, p.om_lo);                                                \
+    h[QM] = relax(h[QM], sym - asym, p.om_hi, p.om_lo);                                                \
   }
-  PLBM_COMP_PAIR(1, 3, ux, jx, 1)
-  PLBM_COMP_PAIR(2, 4, uy, jy, 1)
-  PLBM_COMP_PAIR(5, 7, ux + uy, add_lazy(jx, jy), 2)
-  PLBM_COMP_PAIR(8, 6, ux - uy, add_lazy(jx, neg(jy)), 2)
+  PLBM_COMP_PAIR(1, 3, ux, jx, s13, d13, 1)
+  PLBM_COMP_PAIR(2, 4, uy, jy, s24, d24, 1)
+  PLBM_COMP_PAIR(5, 7, ux + uy, add_lazy(jx, jy), s57, d57, 2)
+  PLBM_COMP_PAIR(8, 6, ux - uy, add_lazy(jx, neg(jy)), s68, d86, 2)
 #undef PLBM_COMP_PAIR
 }
 
