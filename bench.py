@@ -24,7 +24,7 @@ steps 1000/5000/20000) and prints its own JSON line; --suite fields times the
 two field kernels around the job (equilibrium, moments) on device-resident
 fields, integer forms and reference expressions ("variants.field_kernels");
 --suite adjoint times the config-5 adjoint alone (1024^2, T = 2000, K = 45,
-binary32 storage; "variants.adjoint_f32dev").
+binary32 storage; "variants.adjoint_f32dev"; --adj-n / --adj-steps shrink it).
 """
 from __future__ import annotations
 
@@ -457,6 +457,8 @@ def main() -> None:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--suite", default=None, choices=["mixed", "fields", "adjoint"])
+    ap.add_argument("--adj-n", type=int, default=1024, help="--suite adjoint: grid edge")
+    ap.add_argument("--adj-steps", type=int, default=2000, help="--suite adjoint: time steps T")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.math is None:
@@ -493,7 +495,8 @@ def main() -> None:
 
     if args.suite == "adjoint":
         if rank == 0:
-            print(json.dumps({"suite": "adjoint", **adjoint_variant(torch, "f32dev")}), flush=True)
+            print(json.dumps({"suite": "adjoint", **adjoint_variant(torch, "f32dev", n=args.adj_n, T=args.adj_steps)}),
+                  flush=True)
         return
 
     if args.suite == "fields":
