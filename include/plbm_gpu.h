@@ -338,8 +338,10 @@ int plbm_batch_download(plbm_batch_t *b, int grid, double *f);
  * checkpoint_every (K) steps and recomputing each segment: ceil(T/K) + 2K + 4
  * lattices, the recomputation of the next segment running on a second stream
  * of the handle beside the reverse steps of the current one (ordered by
- * events; the call's work still ends on the caller's stream).  dL/domega is
- * accumulated in binary64.  storage PLBM_F64 (binary64 arithmetic) or
+ * events; the call's work still ends on the caller's stream).  When the
+ * second K-lattice buffer does not fit, create falls back to one buffer,
+ * each recomputation after the previous sweep (same gradients, bit for bit).
+ * dL/domega is accumulated in binary64.  storage PLBM_F64 (binary64 arithmetic) or
  * PLBM_F32DEV (binary32 storage and per-cell arithmetic).
  * All field pointers are DEVICE arrays of 2*nx*ny doubles: component a of
  * cell (x,y) at a*nx*ny + y + ny*x (two (ny,nx) fields). */

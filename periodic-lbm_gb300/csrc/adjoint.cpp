@@ -11,9 +11,12 @@
 // its buffer, and each reverse sweep after its recomputation).  The two
 // kernels' streams share the SMs and HBM: neither fills the GPU alone at
 // 1024^2 (tails of 4096-CTA launches, load latency).  Device memory:
-// (ceil(T/K) + 2K + 4) lattices with more than one segment.  Each forward
+// (ceil(T/K) + 2K + 4) lattices with more than one segment; when the second
+// buffer does not fit, one buffer and each recomputation after the previous
+// sweep (ceil(T/K) + K + 4).  Each forward
 // step is computed twice in all (forward pass + recomputation).
 #include <cuda_runtime.h>
+#include <stdlib.h>
 #include <string.h>
 #include <vector>
 
@@ -40,7 +43,7 @@ struct plbm_adjoint {
   int nx, ny, ld, storage, nsteps, K, nck, device;
   size_t lat_bytes;
   char* ck = nullptr;    // nck lattices
-  char* seg = nullptr;   // nseg x K lattices (nseg = 2 with more than one segment)
+  char* seg = nullptr;   // nseg x K lattices (nseg = 2 with more than one segment, 1 if 2 do not fit)
   char* work = nullptr;  // 2 lattices
   char* lam = nullptr;   // 2 lattices
   double* u0 = nullptr;  // 2*nx*ny
@@ -108,9 +111,19 @@ extern "C" int plbm_adjoint_create(int nx, int ny, int storage, int nsteps, int 
   cudaGetDevice(&a->device);
   a->lat_bytes = (size_t)a->ld * nx * 9 * (storage == PLBM_F64 ? 8 : 4);
   a->nblocks = adjoint_blocks(nx, ny);
-  a->nseg = a->nck > 1 ? 2 : 1;
+  // PLBM_ADJOINT_ONE_SEGMENT=1 takes the one-buffer schedule (the fallback
+  // below) for tests
+  const char* one = getenv("PLBM_ADJOINT_ONE_SEGMENT");
+  a->nseg = (a->nck > 1 && !(one && one[0] == '1')) ? 2 : 1;
   cudaError_t e = cudaMalloc(&a->ck, a->lat_bytes * a->nck);
-  if (e == cudaSuccess) e = cudaMalloc(&a->seg, a->lat_bytes * a->K * a->nseg);
+  if (e == cudaSuccess) {
+    e = cudaMalloc(&a->seg, a->lat_bytes * a->K * a->nseg);
+    if (e == cudaErrorMemoryAllocation && a->nseg == 2) {  // one buffer: recomputation after each sweep
+      cudaGetLastError();
+      a->nseg = 1;
+      e = cudaMalloc(&a->seg, a->lat_bytes * a->K);
+    }
+  }
   if (e == cudaSuccess) e = cudaMalloc(&a->work, a->lat_bytes * 2);
   if (e == cudaSuccess) e = cudaMalloc(&a->lam, a->lat_bytes * 2);
   if (e == cudaSuccess) e = cudaMalloc(&a->u0, sizeof(double) * 2 * (size_t)nx * ny);
@@ -232,7 +245,7 @@ extern "C" int plbm_adjoint_backward(plbm_adjoint_t* a, const double* grad_uT, d
   if (rc != PLBM_OK) return rc;
   int li = 0;
   for (int k = a->nck - 1; k >= 0; k--) {
-    if (k >= 1) {
+    if (k >= 1 && a->nseg == 2) {
       // segment k-1 reuses the buffer of segment k+1: after its reverse sweep
       if (k + 1 < a->nck) CUDA_TRY(cudaStreamWaitEvent(a->side, a->ev_rev[(k + 1) & 1], 0), "wait reverse sweep");
       rc = recompute(k - 1);
@@ -250,6 +263,11 @@ extern "C" int plbm_adjoint_backward(plbm_adjoint_t* a, const double* grad_uT, d
       li = 1 - li;
     }
     CUDA_TRY(cudaEventRecord(a->ev_rev[k & 1], a->stream), "record reverse sweep");
+    if (k >= 1 && a->nseg == 1) {  // one buffer: segment k-1 after the sweep of segment k
+      CUDA_TRY(cudaStreamWaitEvent(a->side, a->ev_rev[k & 1], 0), "wait reverse sweep");
+      rc = recompute(k - 1);
+      if (rc != PLBM_OK) return rc;
+    }
   }
   // join: nothing of the side stream outlives the call's work on the caller's stream
   CUDA_TRY(cudaEventRecord(a->ev_join, a->side), "record join");
