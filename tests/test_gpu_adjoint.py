@@ -168,8 +168,9 @@ def test_config5_gradient_against_central_differences_full_size(gpu_lib):
     dL/dtau of L = 1/2 |u_T - u*|^2 from the binary64 discrete adjoint against
     central differences (h = 1e-4) of the binary64 forward model on 32 seeded
     random components of u0 and on tau, each within 1e-5 relative; then the
-    binary32-storage model's adjoint gradient against the binary64 one (its
-    relative error is printed; the bench records it)."""
+    binary32-storage model's adjoint gradient against the binary64 one: within
+    5e-5 (dL/du0, norm-wise) and 1.5e-4 (dL/dtau) of it (the bench records the
+    figures)."""
     import torch
     from plbm.autograd import Adjoint
     n, T, K, tau, h = 1024, 2000, 45, 0.8, 1e-4
@@ -209,4 +210,5 @@ def test_config5_gradient_against_central_differences_full_size(gpu_lib):
     rel32 = float(torch.linalg.norm(g32 - g64) / torch.linalg.norm(g64))
     rel32_tau = abs(-dom32 / tau ** 2 - gtau) / abs(gtau)
     print(f"config 5: binary32-storage gradient vs binary64: dL/du0 {rel32:.2e}, dL/dtau {rel32_tau:.2e}")
-    assert rel32 <= 1e-2 and rel32_tau <= 1e-2
+    # measured 3.0e-5 and 8.0e-5 (both runs are deterministic: fixed-order sums)
+    assert rel32 <= 5e-5 and rel32_tau <= 1.5e-4
