@@ -412,34 +412,45 @@ def adjoint_variant(torch, storage, n=1024, T=2000, K=45):
     tx, ty = cases.divergence_free_modes(n, 16, 8, 0.01, seed=2)
     u0 = torch.tensor(np.stack([ux, uy]), device="cuda")
     tgt = torch.tensor(np.stack([tx, ty]), device="cuda")
-    a = Adjoint(n, n, T, K, storage)
-    uT = a.forward(u0, 1 / 0.8)
-    a.backward(uT - tgt)
-    torch.cuda.synchronize()
-    e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
-    e[0].record()
-    uT = a.forward(u0, 1 / 0.8)
-    e[1].record()
-    a.backward(uT - tgt)
-    e[2].record()
-    torch.cuda.synchronize()
-    f_ms, b_ms = e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2])
-    mem = a.memory_bytes()
-    g32, dom32 = a.backward(uT - tgt)
-    a.close()
+
+    def timed(math_mode):
+        a = Adjoint(n, n, T, K, storage, math=math_mode)
+        uT = a.forward(u0, 1 / 0.8)
+        a.backward(uT - tgt)
+        torch.cuda.synchronize()
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        e[0].record()
+        uT = a.forward(u0, 1 / 0.8)
+        e[1].record()
+        a.backward(uT - tgt)
+        e[2].record()
+        torch.cuda.synchronize()
+        f_ms, b_ms = e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2])
+        mem = a.memory_bytes()
+        g, dom = a.backward(uT - tgt)
+        a.close()
+        return f_ms, b_ms, mem, g, dom
+
+    f_ms, b_ms, mem, g32, dom32 = timed("fma")
+    fc_ms, bc_ms, _, gc, domc = timed("hybrid")
     # the binary64 model's adjoint gradient of the same problem: the binary32
-    # storage gradient's error against it (dL/du0 norm-wise, dL/dtau)
+    # storage gradients' errors against it (dL/du0 norm-wise, dL/dtau)
     a64 = Adjoint(n, n, T, K, "f64")
     uT64 = a64.forward(u0, 1 / 0.8)
     g64, dom64 = a64.backward(uT64 - tgt)
     a64.close()
     torch.cuda.synchronize()
-    err_u0 = float(torch.linalg.norm(g32 - g64) / torch.linalg.norm(g64))
-    err_tau = abs(dom32 - dom64) / abs(dom64)  # dL/dtau = -dL/domega tau^2: the same relative error
+
+    def errs(g, dom):  # dL/dtau = -dL/domega tau^2: the same relative error
+        return {"du0_l2": float(torch.linalg.norm(g - g64) / torch.linalg.norm(g64)),
+                "dtau": abs(dom - dom64) / abs(dom64)}
+
     return {"grid": [n, n], "steps": T, "checkpoint_every": K, "storage": storage, "forward_ms": f_ms,
             "backward_ms": b_ms, "adjoint_over_forward": b_ms / f_ms, "device_GB": mem / 1e9,
-            "grad_rel_err_f32_vs_f64": {"du0_l2": err_u0, "dtau": err_tau,
-                                        "against": "binary64 discrete adjoint of the same problem"}}
+            "grad_rel_err_f32_vs_f64": dict(errs(g32, dom32), against="binary64 discrete adjoint of the same problem"),
+            "compensated_reverse_step": {"forward_ms": fc_ms, "backward_ms": bc_ms, "adjoint_over_forward": bc_ms / fc_ms,
+                                         "grad_rel_err_f32_vs_f64": errs(gc, domc),
+                                         "math": "plbm_adjoint_set_math(PLBM_MATH_HYBRID)"}}
 
 
 def main() -> None:

@@ -53,6 +53,7 @@ struct plbm_adjoint {
   const void* fT = nullptr;
   int have_forward = 0;
   int nseg = 1;
+  int math = PLBM_MATH_FMA;  // reverse-step arithmetic (plbm_adjoint_set_math)
   cudaStream_t own = nullptr, stream = nullptr;
   cudaStream_t side = nullptr;          // recomputation stream
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_rec[2] = {nullptr, nullptr}, ev_rev[2] = {nullptr, nullptr};
@@ -78,6 +79,7 @@ AdjLaunch base_launch(const plbm_adjoint_t* a) {
   L.ny = a->ny;
   L.ld = a->ld;
   L.omega = a->omega;
+  L.comp = a->storage == PLBM_F32DEV && a->math == PLBM_MATH_HYBRID;
   L.stream = a->stream;
   return L;
 }
@@ -170,6 +172,16 @@ extern "C" int plbm_adjoint_set_stream(plbm_adjoint_t* a, void* stream) {
   if (!a) return fail(PLBM_E_INVALID, "NULL adjoint");
   a->stream = stream ? static_cast<cudaStream_t>(stream) : a->own;
   return PLBM_OK;
+}
+
+extern "C" int plbm_adjoint_set_math(plbm_adjoint_t* a, int math) {
+  if (!a) return fail(PLBM_E_INVALID, "NULL adjoint");
+  if (math == PLBM_MATH_FMA || (math == PLBM_MATH_HYBRID && a->storage == PLBM_F32DEV)) {
+    a->math = math;
+    return PLBM_OK;
+  }
+  return fail(PLBM_E_UNSUPPORTED, "adjoint math %d with storage %d (PLBM_MATH_FMA, or PLBM_MATH_HYBRID for PLBM_F32DEV)",
+              math, a->storage);
 }
 
 extern "C" int plbm_adjoint_memory(const plbm_adjoint_t* a, size_t* bytes) {

@@ -13,7 +13,9 @@
 //   S0 = sum w_q lambda_q, A = sum w_q lambda_q (1 - 4.5 (c_q.u)^2 + 1.5 u^2),
 //   B = sum w_q lambda_q (3 + 9 c_q.u) c_q.
 // The per-cell adjoint arithmetic runs in the storage's type (binary64 for
-// PLBM_F64, binary32 for PLBM_F32DEV): lambda, its weighted sums and mu.  The
+// PLBM_F64, binary32 for PLBM_F32DEV): lambda, its weighted sums and mu; with
+// plbm_adjoint_set_math(PLBM_MATH_HYBRID) the binary32 reverse step is the
+// compensated one of coll_df64.cuh (k_adj_step_comp).  The
 // gradients are accumulated in binary64: each cell's dL/domega term is taken
 // to binary64 and summed over the warp in binary64 into the warp's own slot
 // (the host adds the slots in a fixed order), and dL/du0 is assembled from
@@ -21,6 +23,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/plbm_gpu.h"
+#include "coll_df64.cuh"
 #include "plbm_adjoint.h"
 #include "plbm_launch.h"
 
@@ -191,6 +194,38 @@ __global__ void __launch_bounds__(kBlock) k_adj_step(const void* __restrict__ f,
   if ((threadIdx.x & 31) == 0) dom[(size_t)blockIdx.x * (kBlock / 32) + (threadIdx.x >> 5)] += t;
 }
 
+// The reverse step in compensated binary32 (binary32 storage; df::adj_step_comp
+// of coll_df64.cuh): the same loads, scatter and dL/domega slots as k_adj_step.
+// Compiled for 4 CTAs of 256 per SM (64 registers): uncapped it takes 73 and
+// runs at 3, capped at 48 it spills; 4 measured fastest.
+template <typename I>
+__global__ void __launch_bounds__(kBlock, 4) k_adj_step_comp(const float* __restrict__ fe, const float* __restrict__ li,
+                                                         float* __restrict__ lo, double* __restrict__ dom,
+                                                         df::AdjDevParams cpar, int nx, int ny, int ld,
+                                                         int ftiles) {
+  int x, y;
+  const bool in = yfast_cell(ftiles, ny, x, y);
+  float part = 0.0f;
+  if (in) {
+    const I L = (I)ld, P = (I)ld * (I)nx;
+    const I c0 = (I)x * L, cm = (I)wrap_m(x, nx) * L, cp = (I)wrap_p(x, nx) * L;
+    const I y0 = (I)y, ym = (I)wrap_m(y, ny), yp = (I)wrap_p(y, ny);
+    const I off[9] = {c0 + y0,         P + cm + y0,     2 * P + c0 + ym, 3 * P + cp + y0, 4 * P + c0 + yp,
+                      5 * P + cm + ym, 6 * P + cp + ym, 7 * P + cp + yp, 8 * P + cm + yp};
+    float g[9], l[9], mu[9];
+#pragma unroll
+    for (int q = 0; q < 9; q++) {
+      g[q] = __ldg(fe + off[q]);
+      l[q] = __ldg(li + ((I)q * P + c0 + y0));
+    }
+    part = df::adj_step_comp(g, l, mu, cpar);
+#pragma unroll
+    for (int q = 0; q < 9; q++) lo[off[q]] = mu[q];
+  }
+  const double t = warp_sum((double)part);
+  if ((threadIdx.x & 31) == 0) dom[(size_t)blockIdx.x * (kBlock / 32) + (threadIdx.x >> 5)] += t;
+}
+
 // dL/du0 from lambda_0 and u0.
 template <int ST>
 __global__ void __launch_bounds__(kBlock) k_adj_u0(const void* __restrict__ lam, const double* __restrict__ u0,
@@ -223,6 +258,25 @@ cudaError_t dispatch(int what, const AdjLaunch& a) {
     case 0: k_adj_init<ST><<<nb, kBlock, 0, a.stream>>>(a.u, const_cast<void*>(a.f), a.nx, a.ny, a.ld, ft); break;
     case 1: k_adj_final<ST><<<nb, kBlock, 0, a.stream>>>(a.f, a.g, a.out, a.lam_out, a.nx, a.ny, a.ld, ft); break;
     case 2:
+      if (ST == ST_F32DEV && a.comp) {
+        df::AdjDevParams cpar;
+        const double w[3] = {W0, WS, WD};
+        for (int i = 0; i < 3; i++) {
+          const float hi = (float)w[i], hi3 = (float)(3.0 * w[i]);
+          cpar.w[i] = df::make(hi, (float)(w[i] - (double)hi));
+          cpar.w3[i] = df::make(hi3, (float)(3.0 * w[i] - (double)hi3));
+        }
+        cpar.om_hi = (float)a.omega;
+        cpar.om_lo = (float)(a.omega - (double)cpar.om_hi);
+        const float* fa = static_cast<const float*>(a.f);
+        const float* la = static_cast<const float*>(a.lam_in);
+        float* lb = static_cast<float*>(a.lam_out);
+        if ((unsigned long long)a.ld * (unsigned long long)a.nx * 9ull < (1ull << 32))
+          k_adj_step_comp<uint32_t><<<nb, kBlock, 0, a.stream>>>(fa, la, lb, a.dom, cpar, a.nx, a.ny, a.ld, ft);
+        else
+          k_adj_step_comp<size_t><<<nb, kBlock, 0, a.stream>>>(fa, la, lb, a.dom, cpar, a.nx, a.ny, a.ld, ft);
+        break;
+      }
       if ((unsigned long long)a.ld * (unsigned long long)a.nx * 9ull < (1ull << 32))
         k_adj_step<ST, uint32_t><<<nb, kBlock, 0, a.stream>>>(a.f, a.lam_in, a.lam_out, a.dom,
                                                               (typename AdjTraits<ST>::real)a.omega, a.nx, a.ny,

@@ -162,5 +162,87 @@ DF_HD void bgk_dev_comp(float (&h)[9], const DevParams& p) {
 #undef PLBM_COMP_PAIR
 }
 
+// ---- compensated binary32 reverse step of the BGK adjoint ---------------------
+// One cell of the discrete adjoint's reverse step on binary32 deviation
+// storage: g = the pulled pre-collision populations (h = f - w), l = lambda_{n+1}
+// at the cell.  Returns mu (the nine values scattered to lambda_n) and the
+// cell's dL/domega term sum_q lambda_q (feq_q - g_q).  The BGK Jacobian
+// transpose, mu_q = lambda_q + omega (X_q - lambda_q) with
+//   X_q = A + c_q.E,  A = S0 - N,  E = 3 M1 + 9 Q - 3 S0 u,
+//   S0 = sum w lambda, M1 = sum w lambda c, Q = sum w lambda (c.u) c,
+//   N = sum w lambda (4.5 (c.u)^2 - 1.5 u^2),
+// is evaluated like the compensated forward collision: S0 and 3 M1 (the O(lambda)
+// terms) in double-float from exact pairwise sums of lambda, Q and N (O(u lambda))
+// in binary32, and X_q - lambda_q of each pair from the pair's exact sum and
+// difference, (S0 - L/2 - N) +- (c.3M1 - D/2 + c.F), so that only the small
+// non-equilibrium part of lambda is rounded before the single rounding of mu.
+// feq_q - g_q takes the forward's pair form.
+struct AdjDevParams {
+  df64 w[3], w3[3];  // w0, ws, wd and 3 w as double-float
+  float om_hi, om_lo;
+};
+
+DF_HD float adj_step_comp(const float (&g)[9], const float (&l)[9], float (&mu)[9], const AdjDevParams& p) {
+  // forward state of the cell
+  const df64 s13 = two_sum(g[1], g[3]), s24 = two_sum(g[2], g[4]);
+  const df64 s57 = two_sum(g[5], g[7]), s68 = two_sum(g[6], g[8]);
+  const df64 d13 = two_sum(g[1], -g[3]), d24 = two_sum(g[2], -g[4]);
+  const df64 d57 = two_sum(g[5], -g[7]), d86 = two_sum(g[8], -g[6]);
+  const df64 drho = add_lazy(add_lazy(add_lazy(s57, s68), add_lazy(s13, s24)), make(g[0], 0.0f));
+  const df64 jx = add_lazy(add_lazy(d57, d86), d13);
+  const df64 jy = add_lazy(add_lazy(d57, neg(d86)), d24);
+  const float dr = drho.hi + drho.lo;
+  const float inv = 1.0f / (1.0f + dr);
+  const float ux = (jx.hi + jx.lo) * inv, uy = (jy.hi + jy.lo) * inv;
+  const float rho = 1.0f + dr;
+  const float u2 = 1.5f * (ux * ux + uy * uy);
+  const float upp = ux + uy, upm = ux - uy;
+  // exact pairwise sums and differences of lambda
+  const df64 L13 = two_sum(l[1], l[3]), L24 = two_sum(l[2], l[4]);
+  const df64 L57 = two_sum(l[5], l[7]), L68 = two_sum(l[6], l[8]);
+  const df64 M13 = two_sum(l[1], -l[3]), M24 = two_sum(l[2], -l[4]);
+  const df64 M57 = two_sum(l[5], -l[7]), M86 = two_sum(l[8], -l[6]);
+  // S0 and 3 M1 in double-float
+  const df64 S0 = add_lazy(add_lazy(mul_lazy(p.w[1], add_lazy(L13, L24)), mul_lazy(p.w[2], add_lazy(L57, L68))),
+                           mul_lazy_f(p.w[0], l[0]));
+  const df64 Mp = add_lazy(M57, M86), Mm = add_lazy(M57, neg(M86));
+  const df64 E3x = add_lazy(mul_lazy(p.w3[1], M13), mul_lazy(p.w3[2], Mp));
+  const df64 E3y = add_lazy(mul_lazy(p.w3[1], M24), mul_lazy(p.w3[2], Mm));
+  // O(u lambda) terms in binary32
+  const float ws = p.w[1].hi, wd = p.w[2].hi;
+  const float l13 = L13.hi + L13.lo, l24 = L24.hi + L24.lo, l57 = L57.hi + L57.lo, l68 = L68.hi + L68.lo;
+  const float s0 = S0.hi + S0.lo;
+  const float Qx = ws * ux * l13 + wd * (upp * l57 + upm * l68);
+  const float Qy = ws * uy * l24 + wd * (upp * l57 - upm * l68);
+  const float N = 4.5f * (ws * (ux * ux * l13 + uy * uy * l24) + wd * (upp * upp * l57 + upm * upm * l68)) - u2 * s0;
+  const float Fx = 9.0f * Qx - 3.0f * s0 * ux, Fy = 9.0f * Qy - 3.0f * s0 * uy;
+  float dterm;
+  {  // rest population
+    const df64 e = mul_lazy(p.w[0], add_lazy(drho, make(rho * -u2, 0.0f)));
+    dterm = l[0] * ((e.hi - g[0]) + e.lo);
+    mu[0] = relax(l[0], ((S0.hi - l[0]) + S0.lo) - N, p.om_hi, p.om_lo);
+  }
+#define PLBM_ADJ_PAIR(QP, QM, CUF, CJ, S, D, WI, LS, LD, E3C, CF)                                      \
+  {                                                                                                   \
+    const float cu = (CUF);                                                                           \
+    const df64 a = mul_lazy(p.w[WI], add_lazy(drho, make(rho * fmaf_(4.5f * cu, cu, -u2), 0.0f)));   \
+    const df64 b = mul_lazy(p.w3[WI], CJ);                                                            \
+    const float sym = fmaf_(-0.5f, S.hi, a.hi) + fmaf_(-0.5f, S.lo, a.lo);                            \
+    const float asym = fmaf_(-0.5f, D.hi, b.hi) + fmaf_(-0.5f, D.lo, b.lo);                           \
+    dterm += (l[QP] + l[QM]) * sym + (l[QP] - l[QM]) * asym;                                          \
+    const df64 e3 = (E3C);                                                                            \
+    const float ls = (fmaf_(-0.5f, LS.hi, S0.hi) + fmaf_(-0.5f, LS.lo, S0.lo)) - N;                   \
+    const float la = (fmaf_(-0.5f, LD.hi, e3.hi) + fmaf_(-0.5f, LD.lo, e3.lo)) + (CF);                \
+    mu[QP] = relax(l[QP], ls + la, p.om_hi, p.om_lo);                                                 \
+    mu[QM] = relax(l[QM], ls - la, p.om_hi, p.om_lo);                                                 \
+  }
+  PLBM_ADJ_PAIR(1, 3, ux, jx, s13, d13, 1, L13, M13, E3x, Fx)
+  PLBM_ADJ_PAIR(2, 4, uy, jy, s24, d24, 1, L24, M24, E3y, Fy)
+  PLBM_ADJ_PAIR(5, 7, upp, add_lazy(jx, jy), s57, d57, 2, L57, M57, add_lazy(E3x, E3y), Fx + Fy)
+  PLBM_ADJ_PAIR(8, 6, upm, add_lazy(jx, neg(jy)), s68, d86, 2, L68, M86, add_lazy(E3x, neg(E3y)), Fx - Fy)
+#undef PLBM_ADJ_PAIR
+  return dterm;
+}
+
 }  // namespace df
 }  // namespace plbm

@@ -14,6 +14,7 @@ struct AdjLaunch {
   double* out;          // u_T or dL/du0, (2,nx,ny)
   double* dom;          // per-block dL/domega slots
   double omega;
+  int comp;             // reverse step in compensated binary32 (binary32 storage)
   cudaStream_t stream;
 };
 

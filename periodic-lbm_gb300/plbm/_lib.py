@@ -127,6 +127,7 @@ SIGNATURES = {
     "plbm_adjoint_create": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(_vp)]),
     "plbm_adjoint_destroy": (C.c_int, [_vp]),
     "plbm_adjoint_set_stream": (C.c_int, [_vp, _vp]),
+    "plbm_adjoint_set_math": (C.c_int, [_vp, C.c_int]),
     "plbm_adjoint_memory": (C.c_int, [_vp, C.POINTER(C.c_size_t)]),
     "plbm_adjoint_forward": (C.c_int, [_vp, _vp, C.c_double, _vp]),
     "plbm_adjoint_backward": (C.c_int, [_vp, _vp, _vp, _dp]),

@@ -10,13 +10,14 @@ Shapes: u0 is a CUDA float64 tensor (2, nx, ny) -- component, x, y with y
 fastest, i.e. the two (ny,nx) Fortran fields of the reference -- and tau a
 0-d float64 tensor (omega = 1/tau).  storage "f64" differentiates the binary64
 model, "f32dev" the binary32 deviation-storage model (gradients still
-accumulated in binary64).  Memory is bounded by checkpointing every
+accumulated in binary64; ``Adjoint(..., math="hybrid")`` runs its reverse step
+in compensated binary32).  Memory is bounded by checkpointing every
 ``checkpoint_every`` steps (default ~sqrt(nsteps)) and recomputing.
 """
 from __future__ import annotations
 
 import ctypes as C
-import math
+from math import sqrt as _sqrt
 
 import torch
 
@@ -28,13 +29,19 @@ class Adjoint:
     """Owner of one plbm_adjoint handle (checkpoints of one forward run)."""
 
     def __init__(self, nx: int, ny: int, nsteps: int, checkpoint_every: int | None = None,
-                 storage: str = "f64"):
+                 storage: str = "f64", math: str = "fma"):
         self._lib = _lib.load()
-        k = checkpoint_every or max(1, int(round(math.sqrt(nsteps))))
+        k = checkpoint_every or max(1, int(round(_sqrt(nsteps))))
         h = C.c_void_p()
         check(self._lib.plbm_adjoint_create(int(nx), int(ny), _lib.STORAGES[storage], int(nsteps), int(k),
                                             C.byref(h)))
         self._h = h
+        if math != "fma":
+            try:
+                check(self._lib.plbm_adjoint_set_math(h, _lib.MATHS[math]))
+            except Exception:
+                self.close()
+                raise
         self.nx, self.ny, self.nsteps, self.checkpoint_every, self.storage = nx, ny, nsteps, k, storage
 
     def close(self):

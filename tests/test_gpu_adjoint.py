@@ -142,6 +142,35 @@ def test_f32_adjoint_close_to_f64_adjoint(gpu_lib):
     assert abs(d32 - d64) <= 1e-3 * abs(d64)
 
 
+def test_compensated_reverse_step_is_closer_to_binary64(gpu_lib):
+    """plbm_adjoint_set_math(PLBM_MATH_HYBRID) on binary32 storage: the
+    compensated reverse step's gradients lie closer to the binary64 adjoint's
+    than the plain binary32 step's, and it is refused for binary64 storage."""
+    import torch
+    from plbm import PlbmError
+    from plbm.autograd import Adjoint
+    nx, ny, steps = 64, 64, 300
+    ux0, uy0 = fields(nx, ny, seed=7)
+    tx, ty = fields(nx, ny, seed=8)
+    u0 = torch.tensor(np.stack([ux0, uy0]), device="cuda")
+    tgt = torch.tensor(np.stack([tx, ty]), device="cuda")
+    out = {}
+    for st, m in (("f64", "fma"), ("f32dev", "fma"), ("f32dev", "hybrid")):
+        a = Adjoint(nx, ny, steps, checkpoint_every=17, storage=st, math=m)
+        uT = a.forward(u0, 1.25)
+        out[st, m] = a.backward(uT - tgt)
+        a.close()
+    g64, d64 = out["f64", "fma"]
+    err = {}
+    for m in ("fma", "hybrid"):
+        g, d = out["f32dev", m]
+        err[m] = (float(torch.linalg.norm(g - g64) / torch.linalg.norm(g64)), abs(d - d64) / abs(d64))
+    print(f"f32dev vs f64 adjoint: plain {err['fma']}, compensated {err['hybrid']}")
+    assert err["hybrid"][0] < err["fma"][0] and err["hybrid"][1] < err["fma"][1]
+    with pytest.raises(PlbmError):
+        Adjoint(16, 16, 10, storage="f64", math="hybrid")
+
+
 def test_adjoint_errors(gpu_lib):
     from plbm import PlbmError
     from plbm.autograd import Adjoint
@@ -169,7 +198,8 @@ def test_config5_gradient_against_central_differences_full_size(gpu_lib):
     central differences (h = 1e-4) of the binary64 forward model on 32 seeded
     random components of u0 and on tau, each within 1e-5 relative; then the
     binary32-storage model's adjoint gradient against the binary64 one: within
-    5e-5 (dL/du0, norm-wise) and 1.5e-4 (dL/dtau) of it (the bench records the
+    5e-5 (dL/du0, norm-wise) and 1.5e-4 (dL/dtau) of it, and with the
+    compensated reverse step within 1.5e-5 and 4e-5 (the bench records the
     figures)."""
     import torch
     from plbm.autograd import Adjoint
@@ -212,3 +242,12 @@ def test_config5_gradient_against_central_differences_full_size(gpu_lib):
     print(f"config 5: binary32-storage gradient vs binary64: dL/du0 {rel32:.2e}, dL/dtau {rel32_tau:.2e}")
     # measured 3.0e-5 and 8.0e-5 (both runs are deterministic: fixed-order sums)
     assert rel32 <= 5e-5 and rel32_tau <= 1.5e-4
+    c = Adjoint(n, n, T, K, "f32dev", math="hybrid")
+    uTc = c.forward(u0, 1.0 / tau)
+    gc, domc = c.backward(uTc - tgt)
+    c.close()
+    relc = float(torch.linalg.norm(gc - g64) / torch.linalg.norm(g64))
+    relc_tau = abs(-domc / tau ** 2 - gtau) / abs(gtau)
+    print(f"config 5: compensated reverse step vs binary64: dL/du0 {relc:.2e}, dL/dtau {relc_tau:.2e}")
+    # measured 9.4e-6 and 2.7e-5
+    assert relc <= 1.5e-5 and relc_tau <= 4e-5
