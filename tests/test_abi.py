@@ -64,6 +64,8 @@ def test_invalid_arguments_are_rejected_without_a_device(lib):
     assert lib.plbm_perform_lbm_step(None, 1) == _lib.PLBM_E_INVALID
     assert lib.plbm_vorticity(3, 4, 4, None, None, None) == _lib.PLBM_E_INVALID
     assert lib.plbm_launch_step(0, 0, 0, 8, 8, 4, None, None, 1.0, 0.25, None) == _lib.PLBM_E_INVALID
+    assert lib.plbm_adjoint_set_math(None, 0) == _lib.PLBM_E_INVALID
+    assert lib.plbm_adjoint_set_stream(None, None) == _lib.PLBM_E_INVALID
 
 
 def test_extents_above_the_32_bit_cell_limit_are_rejected(lib):
