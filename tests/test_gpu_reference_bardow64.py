@@ -11,7 +11,10 @@ and must print the same digits: the fused stencil form with FMA arithmetic
 and the fused hybrid collision at every point (17,558 to 1,755,763 steps),
 the strict build (the reference's operations in order, two passes per step;
 bit-identical to the oracle) at the points with dt/tau >= 1.5.  A point
-takes 0.1 - 26 s on a GB300.
+takes 0.1 - 12 s on a GB300 (the 56 cases about 2.5 minutes).  "The same
+digits" allows half a printed unit plus 3e-10 (reference_tgv.NOISE): the
+spread between builds of the same arithmetic with and without FMA
+contraction.
 """
 from __future__ import annotations
 
